@@ -1,0 +1,366 @@
+"""Benchmark of the GB300 force engine (one JSON line on stdout).
+
+Workload (N = 1): direct-sum gravity, N = 131072 Plummer sphere (scale radius
+1, total mass 1, equal masses, isotropic velocities, seeded), softening 1e-3,
+FP32 pair math with compensated (two-sum) accumulation and FP64 state.
+One step = one rk4 step through the engine interface (4 fcompute + 3 fmadd
++ 1 fused fmaddn_inplace).  Metric: direct-sum pair interactions per second
+(4 N^2 pairs per step, the self pair counted as the reference GPU kernel does).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's CPU implementation of the same path
+(the block engine restated in oracle/, all host threads) on a bounded sample
+of rows of the same workload; it runs on rank 0 only.
+
+Multi-GPU: the path is run as independent replicas (one per rank); value is
+the sum over ranks of the pairs processed divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_BODIES = 131072
+SOFTENING = 1e-3
+DT = 1e-3
+FLOP_PER_PAIR = 20  # conventional count (Nyland, Harris & Prins, GPU Gems 3 ch. 31)
+METRIC = "direct pairs/s"
+WORKLOAD = "direct-sum rk4 step, N=131072 Plummer, softening 1e-3, FP32 pairs + two-sum, FP64 state"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=N_BODIES)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas; no data-path collective)
+# ---------------------------------------------------------------------------
+def dist_setup(gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return rank, local, world
+    return 0, 0, 1
+
+
+def dist_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (oracle port of the block engine, host cores)
+# ---------------------------------------------------------------------------
+def cpu_pairs_per_s(y, mass, target_s: float, threads: int):
+    """Time the block engine restatement on a row sample sized to ~target_s."""
+    from oracle.oracle import load_oracle
+    orc = load_oracle()
+    n = mass.size
+    f = np.zeros_like(y)
+    rows = 256
+    t0 = time.perf_counter()
+    orc.fcompute_block_range(y, mass, f, 0, rows, threads)
+    dt = time.perf_counter() - t0
+    rows = int(min(n, max(256, rows * target_s / max(dt, 1e-6))))
+    rows = (rows // 64) * 64 or 64
+    t0 = time.perf_counter()
+    orc.fcompute_block_range(y, mass, f, 0, rows, threads)
+    dt = time.perf_counter() - t0
+    return rows * n / dt, rows, dt
+
+
+def run_reference(args):
+    rank, _, world = int(os.environ.get("RANK", "0")), 0, int(os.environ.get("WORLD_SIZE", "1"))
+    if rank != 0:
+        return
+    from nbody_gb300.data import NBodyData
+    threads = os.cpu_count() or 1
+    d = NBodyData.plummer(args.n, seed=1)
+    y, mass = d.to_state(), d.mass
+    vals = []
+    rows_used = 0
+    t_start = time.perf_counter()
+    for k in range(args.warmup + args.steps):
+        v, rows_used, _ = cpu_pairs_per_s(y, mass, 3.0, threads)
+        if k >= args.warmup:
+            vals.append(v)
+    value = float(np.mean(vals))
+    per_step_ms = 4.0 * args.n * args.n / value * 1e3
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": WORKLOAD, "n": args.n,
+                   "cpu": "block engine (nbody/nbody_engine_block.cpp) restated in oracle/, "
+                          "OpenMP over host cores; the reference itself needs Qt (absent)"},
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
+                         "sample": f"{rows_used} of {args.n} rows x {args.n} bodies per step"},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "wall_s": time.perf_counter() - t_start,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm
+# ---------------------------------------------------------------------------
+def read_traffic():
+    """Per-launch DRAM bytes of the direct kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "direct_mixed_kernel_n131072.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def run_gb300(args):
+    rank, local, world = dist_setup(args.gpus)
+    import torch
+    from nbody_gb300 import _lib
+    from nbody_gb300.data import NBodyData
+    from nbody_gb300.engine import HostBuffer, create_engine
+    from nbody_gb300.solvers import create_solver
+
+    torch.cuda.set_device(local)
+    n = args.n
+    d = NBodyData.plummer(n, seed=1 + rank)
+    e = create_engine({"engine": "gb300", "precision": "mixed", "softening": SOFTENING,
+                       "device": local})
+    if e is None:
+        raise RuntimeError("GB300 engine could not be created")
+    assert e.init(d)
+    s = create_solver({"solver": "rk4"})
+    s.set_time_step(DT, DT)
+    s.set_engine(e)
+    stream = torch.cuda.ExternalStream(_lib.load().nbg_stream(e.handle))
+    flush = e.create_buffer(256 << 20)  # > L2 (129 MB): written between timed steps
+
+    for _ in range(args.warmup):
+        s.advise(DT)
+    e.synchronize()
+
+    # ---- device-timed steps (inputs resident in HBM) ----
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(world)
+    torch.cuda.synchronize()
+    e.synchronize()
+    l0 = e.launch_count()
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        e.fill_buffer(flush, float(k))
+        starts[k].record(stream)
+        s.advise(DT)
+        ends[k].record(stream)
+    e.synchronize()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = e.launch_count() - l0 - args.steps  # minus the L2 flush fills
+    barrier(world)
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    local_ms = float(np.mean(step_ms))
+    ms = dist_max(local_ms, world)
+    pairs_step = 4.0 * n * n
+    value = world * pairs_step / (ms * 1e-3)
+
+    # ---- kernel-level roofline of the direct kernel ----
+    e.profile_enable(True)
+    for _ in range(3):
+        s.advise(DT)
+    kms, klaunch = e.profile_query(_lib.K_DIRECT)
+    e.profile_enable(False)
+    k_avg_s = kms / max(klaunch, 1) * 1e-3
+    achieved_tflops = n * n * FLOP_PER_PAIR / k_avg_s / 1e12
+    peak_flops = e.measure_fp32_peak()
+    props = torch.cuda.get_device_properties(local)
+    nominal = props.multi_processor_count * 128 * 2 * 2.07e9
+
+    # ---- force error of the mixed path vs the FP64 oracle on sampled rows ----
+    err = None
+    if rank == 0:
+        from oracle.oracle import load_oracle
+        orc = load_oracle()
+        y = np.zeros(6 * n)
+        e.read_buffer(y, e.get_y())
+        f = e.create_buffer(8 * 6 * n)
+        e.fcompute(0.0, e.get_y(), f)
+        fo = np.zeros(6 * n)
+        e.read_buffer(fo, f)
+        rows = np.random.default_rng(5).choice(n, size=512, replace=False)
+        a_ref = orc.accel_rows(y, d.mass, SOFTENING, rows=rows)
+        a = fo[3 * n:].reshape(3, n).T[rows]
+        rel = np.linalg.norm(a - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
+        err = {"rms": float(np.sqrt(np.mean(rel ** 2))), "p99": float(np.quantile(rel, 0.99)),
+               "max": float(rel.max()), "sample_rows": 512, "judge": "FP64 direct sum (oracle)"}
+        e.free_buffer(f)
+
+    # ---- end to end through the public API with host buffers ----
+    hy = HostBuffer(6 * n)
+    e.read_buffer(hy.array, e.get_y())
+    e2e_times = []
+    barrier(world)
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        e.write_buffer(e.get_y(), hy.array)
+        s.advise(DT)
+        e.read_buffer(hy.array, e.get_y())
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = dist_max(float(np.mean(e2e_times)), world)
+    e2e_value = world * pairs_step / e2e_s
+    hy.free()
+
+    # ---- CPU baseline on rank 0 ----
+    cpu = None
+    if rank == 0 and world == 1:
+        y = d.to_state()
+        v, rows, dt = cpu_pairs_per_s(y, d.mass, 8.0, os.cpu_count() or 1)
+        cpu = {"value": v, "unit": "pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"block engine (FP64) on {rows} of {n} rows x {n} bodies, {dt:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n": n, "softening": SOFTENING, "dt": DT,
+                       "integrator": "rk4", "precision": "f32 pairs, two-sum tiles, f64 state",
+                       "l2": "flushed between timed steps (256 MB write)",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "fp32", "achieved": achieved_tflops,
+                         "peak": peak_flops / 1e12, "unit": "TFLOP/s",
+                         "frac": achieved_tflops / (peak_flops / 1e12),
+                         "peak_note": "measured FFMA probe on this GPU (no FP32 entry in "
+                                      "MEASURED_PEAKS.json); nominal %.1f TFLOP/s at 2070 MHz"
+                                      % (nominal / 1e12),
+                         "frac_of_nominal": achieved_tflops * 1e12 / nominal,
+                         "kernel": "direct_mixed_kernel",
+                         "kernel_ms": k_avg_s * 1e3,
+                         "flop_per_pair": FLOP_PER_PAIR,
+                         "traffic": read_traffic()},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": 6 * n * 8,
+                    "d2h_bytes_per_step": 6 * n * 8},
+            "gpu_launches": int(launches),
+            "clocks": clk,
+            "force_error": err,
+            "wall_s_timed": wall,
+        }
+        print(json.dumps(line), flush=True)
+    e.free_buffer(flush)
+    e.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

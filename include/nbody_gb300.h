@@ -1,0 +1,178 @@
+/*
+ * nbody_gb300.h -- C ABI of the GB300 force engine for drons/nbody.
+ *
+ * The engine is a drop-in for the reference's `nbody_engine` interface
+ * (nbody/nbody_engine.h:16-96): a reference-side adapter class subclasses
+ * nbody_engine, registers under a new alias in nbody_create_engine
+ * (nbody/nbody_engines.cpp:4-193) and forwards every virtual to the entry
+ * point named beside it below.  Plain pointers and sizes only; every call
+ * returns an nbg_status (the reference's CUDACHECK exit(3) becomes a status
+ * plus a message from nbg_last_error).  One engine = one GPU, one stream.
+ *
+ * Buffers are engine-owned device allocations (the reference's `memory`
+ * subclass, nbody/nbody_engine_cuda_memory.cpp:4-22).  Vector operations act
+ * on size()/8 doubles of their first operand, as the reference CUDA engine
+ * does (nbody/nbody_engine_cuda.cpp:368-530).  A handle that this engine did
+ * not create is rejected with NBG_ERR_FOREIGN_BUFFER and no side effect --
+ * the reference logs "x is not smemory" and returns
+ * (test/engine/test_nbody_engine.cpp:761-1010).
+ */
+#ifndef NBODY_GB300_H
+#define NBODY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NBG_ABI_VERSION 1
+
+typedef enum nbg_status {
+    NBG_OK = 0,
+    NBG_ERR_INVALID_ARG = 1,     /* NULL or out-of-range argument */
+    NBG_ERR_FOREIGN_BUFFER = 2,  /* handle not created by this engine */
+    NBG_ERR_SIZE_MISMATCH = 3,   /* buffer smaller than the operation needs */
+    NBG_ERR_OUT_OF_MEMORY = 4,   /* device or pinned allocation failed */
+    NBG_ERR_CUDA = 5,            /* CUDA runtime error (message in last_error) */
+    NBG_ERR_UNSUPPORTED = 6,     /* e.g. Barnes-Hut with N not a power of two */
+    NBG_ERR_NOT_INITIALIZED = 7, /* nbg_init has not been called */
+    NBG_ERR_DEVICE_TIMEOUT = 8,  /* a bounded device-side wait gave up */
+    NBG_ERR_DEVICE_ERROR = 9     /* a kernel reported an error flag */
+} nbg_status;
+
+typedef struct nbg_engine nbg_engine; /* opaque engine */
+typedef struct nbg_buffer nbg_buffer; /* opaque device buffer */
+
+enum nbg_algo { NBG_ALGO_DIRECT = 0, NBG_ALGO_BH = 1 };
+enum nbg_precision {
+    NBG_PREC_FP64 = 0,  /* FP64 pair math, reference operation order */
+    NBG_PREC_MIXED = 1  /* FP32 pair math, compensated FP32 sums, FP64 state */
+};
+enum nbg_tree_layout { NBG_LAYOUT_HEAP = 1, NBG_LAYOUT_HEAP_STACKLESS = 2 };
+enum nbg_traverse { NBG_TRAVERSE_CYCLE = 0, NBG_TRAVERSE_NESTED_TREE = 1 };
+
+/* Engine parameters: the keys nbody_create_engine reads from its QVariantMap
+ * (nbody/nbody_engines.cpp:21-76) plus the new engine's own keys. */
+typedef struct nbg_params {
+    uint32_t struct_size;       /* sizeof(nbg_params), set by nbg_params_default */
+    int32_t device;             /* CUDA device ordinal ("device", default 0) */
+    int32_t algo;               /* nbg_algo */
+    int32_t precision;          /* nbg_precision */
+    double softening;           /* Plummer epsilon; 0 = reference clamp r^2>=1e-8 only */
+    double distance_to_node_radius_ratio; /* lambda = 1/theta (default 10) */
+    uint64_t tree_build_rate;   /* 0 = rebuild every fcompute, else refit between builds */
+    int32_t tree_layout;        /* nbg_tree_layout (default heap_stackless) */
+    int32_t traverse_type;      /* nbg_traverse (default nested_tree) */
+    int32_t learned;            /* 1 = apply the learned monopole correction (BH, mixed) */
+    int32_t block_size;         /* accepted for key compatibility; must be 0 or >0 */
+    double learned_tight_ratio; /* tight opening ratio lambda_t of the learned band (default 2) */
+} nbg_params;
+
+void nbg_params_default(nbg_params* p);
+const char* nbg_status_string(nbg_status s);
+int nbg_abi_version(void);
+
+/* nbody_create_engine(param) for the new alias (nbody/nbody_engines.cpp:4) */
+nbg_status nbg_engine_create(const nbg_params* p, nbg_engine** out);
+/* ~nbody_engine */
+void nbg_engine_destroy(nbg_engine* e);
+/* nbody_engine::type_name (nbody/nbody_engine.h:40) */
+const char* nbg_type_name(const nbg_engine* e);
+/* Message of the last failing call on this engine ("" if none). */
+const char* nbg_last_error(const nbg_engine* e);
+
+/* nbody_engine::init (nbody/nbody_engine.h:43; nbody_engine_cuda.cpp:91-139).
+ * vertices/velocities are AoS [count][3] like nbody_data. */
+nbg_status nbg_init(nbg_engine* e, size_t count, const double* vertices,
+                    const double* velocities, const double* mass);
+/* nbody_engine::get_data (nbody/nbody_engine.h:45): engine y -> AoS arrays */
+nbg_status nbg_get_data(nbg_engine* e, double* vertices, double* velocities);
+/* nbody_engine::problem_size (= 6 N) and get_y */
+size_t nbg_problem_size(const nbg_engine* e);
+nbg_buffer* nbg_get_y(nbg_engine* e);
+
+/* nbody_engine::fcompute (nbody/nbody_engine.h:61): f = [v ; a(y)].
+ * `step` is the caller's nbody_data step, read by the tree_build_rate rule
+ * (nbody/nbody_engine_simple_bh.cpp:53-60). */
+nbg_status nbg_fcompute(nbg_engine* e, double t, uint64_t step,
+                        const nbg_buffer* y, nbg_buffer* f);
+/* nbody_engine::clamp (nbody/nbody_engine.h:63; nbody_engine_cuda_impl.cu:724-747) */
+nbg_status nbg_clamp(nbg_engine* e, nbg_buffer* y, double b);
+
+/* nbody_engine::create_buffer / free_buffer (nbody/nbody_engine.h:65-66) */
+nbg_status nbg_create_buffer(nbg_engine* e, size_t bytes, nbg_buffer** out);
+nbg_status nbg_free_buffer(nbg_engine* e, nbg_buffer* b);
+/* nbody_engine::memory::size (nbody/nbody_engine.h:27) */
+size_t nbg_buffer_size(const nbg_buffer* b);
+/* Raw device address of a buffer (for callers that launch their own work). */
+void* nbg_buffer_device_ptr(nbg_buffer* b);
+/* read_buffer / write_buffer (nbody/nbody_engine.h:69-70): copy size() bytes.
+ * read_buffer returns after the copy has landed in dst. */
+nbg_status nbg_read_buffer(nbg_engine* e, void* dst, const nbg_buffer* src);
+nbg_status nbg_write_buffer(nbg_engine* e, nbg_buffer* dst, const void* src);
+/* copy_buffer a = b, equal sizes (nbody/nbody_engine_cuda.cpp:318-345) */
+nbg_status nbg_copy_buffer(nbg_engine* e, nbg_buffer* a, const nbg_buffer* b);
+/* fill_buffer a[i] = value over size()/8 doubles */
+nbg_status nbg_fill_buffer(nbg_engine* e, nbg_buffer* a, double value);
+/* fmadd_inplace a[i] += b[i]*c (nbody/nbody_engine.h:76) */
+nbg_status nbg_fmadd_inplace(nbg_engine* e, nbg_buffer* a, const nbg_buffer* b,
+                             double c);
+/* fmadd a[i] = b[i] + c[i]*d (nbody/nbody_engine.h:78) */
+nbg_status nbg_fmadd(nbg_engine* e, nbg_buffer* a, const nbg_buffer* b,
+                     const nbg_buffer* c, double d);
+/* fmaddn_inplace a[i] += sum_k b[k][i]*c[k], one fused pass
+ * (nbody/nbody_engine.cpp:47-66: c == NULL is a no-op, zero c[k] skipped,
+ * csize > bcount is an error). */
+nbg_status nbg_fmaddn_inplace(nbg_engine* e, nbg_buffer* a,
+                              const nbg_buffer* const* b, size_t bcount,
+                              const double* c, size_t csize);
+/* fmaddn_corr: Kahan-compensated fmaddn_inplace with per-element carry
+ * (nbody/nbody_engine_simple.cpp:341-394) */
+nbg_status nbg_fmaddn_corr(nbg_engine* e, nbg_buffer* a, nbg_buffer* corr,
+                           const nbg_buffer* const* b, size_t bcount,
+                           const double* c, size_t csize);
+/* fmaddn a[i] = b[i] + sum_k c[k][i]*d[k]; b == NULL means a = sum
+ * (nbody/nbody_engine.cpp:75-115), one fused pass */
+nbg_status nbg_fmaddn(nbg_engine* e, nbg_buffer* a, const nbg_buffer* b,
+                      const nbg_buffer* const* c, size_t ccount,
+                      const double* d, size_t dsize);
+/* fmaxabs result = max |a[i]| (0 for an empty buffer) */
+nbg_status nbg_fmaxabs(nbg_engine* e, const nbg_buffer* a, double* result);
+
+/* Wait for all work queued on the engine stream; reports device error flags. */
+nbg_status nbg_synchronize(nbg_engine* e);
+/* The engine's CUDA stream (cudaStream_t) for callers that order their own work. */
+void* nbg_stream(nbg_engine* e);
+
+/* Page-locked host memory for fast write_buffer / read_buffer. */
+nbg_status nbg_host_alloc(size_t bytes, void** out);
+void nbg_host_free(void* p);
+
+/* ---- measurement (no reference counterpart) ---- */
+/* Kernel ids for nbg_profile_query. */
+enum nbg_kernel_id {
+    NBG_K_DIRECT = 0,     /* direct-sum force kernel (either precision) */
+    NBG_K_TREE_BUILD = 1, /* whole tree build/refit sequence */
+    NBG_K_BH_WALK = 2,    /* Barnes-Hut traversal kernel */
+    NBG_K_VECOPS = 3,     /* buffer algebra kernels */
+    NBG_K_COUNT = 8
+};
+/* Enable CUDA-event timing of each kernel class on the engine stream. */
+nbg_status nbg_profile_enable(nbg_engine* e, int enable);
+/* Accumulated device time (ms) and launches of one kernel class; resets it. */
+nbg_status nbg_profile_query(nbg_engine* e, int kernel_id, double* total_ms,
+                             uint64_t* launches);
+/* Number of kernels this engine has launched since creation. */
+uint64_t nbg_launch_count(const nbg_engine* e);
+
+/* FP32 FFMA throughput probe: runs a dependent-chain FMA kernel on the
+ * engine's device and returns the measured FP32 FLOP/s (2 per FMA). */
+nbg_status nbg_measure_fp32_peak(nbg_engine* e, double* flops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBODY_GB300_H */

@@ -1,0 +1,338 @@
+// nbg_direct.cu -- direct O(N^2) gravity: f = [v ; a(y)].
+//
+// Two kernels share the engine entry point:
+//
+//  * FP64 (parity) -- one thread per body, j-tiles of double4 in shared
+//    memory, the reference 'simple' arithmetic in the reference order
+//    (nbody/nbody_engine_simple.cpp:143-172 with nbody_data::force,
+//    nbody/nbody_data.cpp:35-44): explicit roundings (no FMA contraction),
+//    self pair skipped, force summed j = 0..N-1 then divided by m_i.
+//
+//  * mixed (throughput) -- FP32 pair math on the FP32 pipe, FP64 state.
+//    A pack kernel turns y into a tile-padded array of bodies in
+//    (x x y y | z z m m) form and writes f = [v ; 0].  The force kernel is
+//    persistent: the (i-block, j-tile) units are split evenly over one wave
+//    of CTAs (stream-K), a producer warp streams j-tiles global -> shared with
+//    1-D bulk async copies (TMA) through an mbarrier ring, and 4 consumer
+//    warps each hold 4 i-bodies per lane in packed FP32x2 registers.  Per
+//    tile the FP32 partial sums are folded into a (hi, lo) two-sum pair; at
+//    the end of an i-block segment hi + lo is added into the FP64 a-part of f
+//    with one atomicAdd per component.  Pair term:
+//        a_i += m_j (r_j - r_i) / (|r_j - r_i|^2 + eps^2)^{3/2}
+//    with r^2 clamped to >= 1e-8 when eps = 0 (the reference clamp).
+#include "nbg_internal.cuh"
+#include "nbg_ptx.cuh"
+
+namespace nbg {
+namespace {
+
+// ---------------------------------------------------------------------------
+// FP64 kernel
+// ---------------------------------------------------------------------------
+constexpr int kF64Threads = 128;
+
+struct alignas(32) D4 {
+    double x, y, z, w;
+};
+
+__global__ void __launch_bounds__(kF64Threads)
+direct_fp64_kernel(const double* __restrict__ y, const double* __restrict__ mass,
+                   double* __restrict__ f, int n) {
+    __shared__ D4 tile[kF64Threads];
+    const int i = blockIdx.x * kF64Threads + threadIdx.x;
+    const bool live = i < n;
+    const double x1 = live ? y[i] : 0.0;
+    const double y1 = live ? y[n + i] : 0.0;
+    const double z1 = live ? y[2 * n + i] : 0.0;
+    const double m1 = live ? mass[i] : 1.0;
+    const double mneg = __dmul_rn(-1.0, m1);
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    for (int j0 = 0; j0 < n; j0 += kF64Threads) {
+        const int j = j0 + threadIdx.x;
+        if (j < n) tile[threadIdx.x] = D4{y[j], y[n + j], y[2 * n + j], mass[j]};
+        __syncthreads();
+        const int cnt = min(kF64Threads, n - j0);
+        for (int k = 0; k < cnt; ++k) {
+            if (j0 + k == i) continue;  // nbody/nbody_engine_simple.cpp:155-158
+            const D4 p = tile[k];
+            const double dx = __dsub_rn(x1, p.x);
+            const double dy = __dsub_rn(y1, p.y);
+            const double dz = __dsub_rn(z1, p.z);
+            double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+            if (r2 < kMinDistance) r2 = kMinDistance;
+            const double c = __ddiv_rn(__dmul_rn(mneg, p.w), __dmul_rn(r2, __dsqrt_rn(r2)));
+            fx = __dadd_rn(fx, __dmul_rn(dx, c));
+            fy = __dadd_rn(fy, __dmul_rn(dy, c));
+            fz = __dadd_rn(fz, __dmul_rn(dz, c));
+        }
+        __syncthreads();
+    }
+    if (live) {
+        f[i] = y[3 * n + i];
+        f[n + i] = y[4 * n + i];
+        f[2 * n + i] = y[5 * n + i];
+        f[3 * n + i] = __ddiv_rn(fx, m1);
+        f[4 * n + i] = __ddiv_rn(fy, m1);
+        f[5 * n + i] = __ddiv_rn(fz, m1);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// mixed kernel
+// ---------------------------------------------------------------------------
+constexpr int kWarps = 4;                      // consumer warps per CTA
+constexpr int kThreadsMixed = (kWarps + 1) * 32;  // + one producer warp
+constexpr int kR = 4;                          // i-bodies per lane (2 packed pairs)
+constexpr int kIB = kWarps * 32 * kR;          // 512 i-bodies per i-block
+constexpr int kT = 128;                        // j-bodies per tile
+constexpr int kStages = 4;                     // tiles in flight
+constexpr uint32_t kTileBytes = kT * 32;       // 32 bytes per body (x x y y z z m m)
+
+struct Body2 {  // one body in duplicated form, 32 bytes
+    float4 xxyy;
+    float4 zzmm;
+};
+
+__global__ void pack_mixed_kernel(const double* __restrict__ y, const double* __restrict__ mass,
+                                  Body2* __restrict__ out, double* __restrict__ f, int n,
+                                  int n_pad) {
+    int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += stride) {
+        Body2 b;
+        if (i < n) {
+            float x = (float)y[i], yy = (float)y[n + i], z = (float)y[2 * n + i];
+            float m = (float)mass[i];
+            b.xxyy = make_float4(x, x, yy, yy);
+            b.zzmm = make_float4(z, z, m, m);
+            f[i] = y[3 * n + i];
+            f[n + i] = y[4 * n + i];
+            f[2 * n + i] = y[5 * n + i];
+            f[3 * n + i] = 0.0;
+            f[4 * n + i] = 0.0;
+            f[5 * n + i] = 0.0;
+        } else {
+            b.xxyy = make_float4(0.f, 0.f, 0.f, 0.f);
+            b.zzmm = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        out[i] = b;
+    }
+}
+
+struct MixedArgs {
+    const Body2* bodies;  // [n_pad]
+    double* acc;          // a-part of f: [3][n]
+    int n;
+    int n_jt;             // j-tiles
+    long long units;      // n_iblocks * n_jt
+    float eps2;
+    unsigned* err;
+};
+
+template <bool CLAMP>
+__device__ __forceinline__ void pair2(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f2_t xi, f2_t yi,
+                                      f2_t zi, f2_t eps2, f2_t& ax, f2_t& ay, f2_t& az) {
+    const f2_t dx = f2_sub(xj, xi);
+    const f2_t dy = f2_sub(yj, yi);
+    const f2_t dz = f2_sub(zj, zi);
+    f2_t r2 = f2_fma(dz, dz, eps2);
+    r2 = f2_fma(dy, dy, r2);
+    r2 = f2_fma(dx, dx, r2);
+    float r2a, r2b;
+    f2_unpack(r2, r2a, r2b);
+    if (CLAMP) {
+        r2a = fmaxf(r2a, 1e-8f);
+        r2b = fmaxf(r2b, 1e-8f);
+    }
+    const f2_t inv = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
+    const f2_t inv2 = f2_mul(inv, inv);
+    const f2_t s = f2_mul(mj, inv);
+    const f2_t s3 = f2_mul(s, inv2);
+    ax = f2_fma(dx, s3, ax);
+    ay = f2_fma(dy, s3, ay);
+    az = f2_fma(dz, s3, az);
+}
+
+template <bool CLAMP>
+__global__ void __launch_bounds__(kThreadsMixed)
+direct_mixed_kernel(MixedArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    Body2* tiles = reinterpret_cast<Body2*>(smem_raw);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + kStages * kTileBytes);
+    uint64_t* empty = full + kStages;
+
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long per = a.units / gridDim.x;
+    const long long rem = a.units % gridDim.x;
+    const long long u0 = blockIdx.x * per + min((long long)blockIdx.x, rem);
+    const long long u1 = u0 + per + ((long long)blockIdx.x < rem ? 1 : 0);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kWarps);
+        }
+        mbar_fence_init();
+    }
+    __syncthreads();
+
+    if (warp == kWarps) {
+        // ---------------- producer warp: one lane issues the bulk copies ------
+        if (lane == 0) {
+            long long k = 0;
+            for (long long u = u0; u < u1; ++u, ++k) {
+                const int s = (int)(k % kStages);
+                const long long round = k / kStages;
+                if (round > 0 && !mbar_wait(&empty[s], (uint32_t)((round - 1) & 1), a.err)) break;
+                const int jt = (int)(u % a.n_jt);
+                mbar_arrive_expect_tx(&full[s], kTileBytes);
+                bulk_g2s(tiles + s * kT, a.bodies + (size_t)jt * kT, kTileBytes, &full[s]);
+            }
+        }
+        return;
+    }
+
+    // -------------------- consumer warps ---------------------------------------
+    const f2_t eps2 = f2_pack(a.eps2, a.eps2);
+    const f2_t zero = f2_pack(0.f, 0.f);
+    f2_t xi[2], yi[2], zi[2];
+    f2_t hx[2], hy[2], hz[2], lx[2], ly[2], lz[2];
+    long long cur_ib = -1;
+    long long k = 0;
+    bool ok = true;
+
+    auto flush = [&](long long ib) {
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+            float h0, h1, l0, l1;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const f2_t hh = c == 0 ? hx[g] : (c == 1 ? hy[g] : hz[g]);
+                const f2_t ll = c == 0 ? lx[g] : (c == 1 ? ly[g] : lz[g]);
+                f2_unpack(hh, h0, h1);
+                f2_unpack(ll, l0, l1);
+                const int i0 = (int)(ib * kIB) + (2 * g) * (kWarps * 32) + warp * 32 + lane;
+                const int i1 = i0 + kWarps * 32;
+                if (i0 < a.n) atomicAdd(a.acc + (size_t)c * a.n + i0, (double)h0 + (double)l0);
+                if (i1 < a.n) atomicAdd(a.acc + (size_t)c * a.n + i1, (double)h1 + (double)l1);
+            }
+        }
+    };
+
+    for (long long u = u0; u < u1; ++u, ++k) {
+        const long long ib = u / a.n_jt;
+        if (ib != cur_ib) {
+            if (cur_ib >= 0) flush(cur_ib);
+            cur_ib = ib;
+#pragma unroll
+            for (int g = 0; g < 2; ++g) {
+                const int i0 = (int)(ib * kIB) + (2 * g) * (kWarps * 32) + warp * 32 + lane;
+                const int i1 = i0 + kWarps * 32;
+                float x0 = 0.f, y0 = 0.f, z0 = 0.f, x1 = 0.f, y1 = 0.f, z1 = 0.f;
+                if (i0 < a.n) {
+                    const Body2 b = a.bodies[i0];
+                    x0 = b.xxyy.x; y0 = b.xxyy.z; z0 = b.zzmm.x;
+                }
+                if (i1 < a.n) {
+                    const Body2 b = a.bodies[i1];
+                    x1 = b.xxyy.x; y1 = b.xxyy.z; z1 = b.zzmm.x;
+                }
+                xi[g] = f2_pack(x0, x1);
+                yi[g] = f2_pack(y0, y1);
+                zi[g] = f2_pack(z0, z1);
+                hx[g] = hy[g] = hz[g] = zero;
+                lx[g] = ly[g] = lz[g] = zero;
+            }
+        }
+        const int s = (int)(k % kStages);
+        const long long round = k / kStages;
+        if (!mbar_wait(&full[s], (uint32_t)(round & 1), a.err)) {
+            ok = false;
+            break;
+        }
+        const Body2* tile = tiles + s * kT;
+        f2_t ax[2] = {zero, zero}, ay[2] = {zero, zero}, az[2] = {zero, zero};
+#pragma unroll 4
+        for (int j = 0; j < kT; ++j) {
+            const float4 p0 = tile[j].xxyy;
+            const float4 p1 = tile[j].zzmm;
+            const f2_t xj = f2_pack(p0.x, p0.y);
+            const f2_t yj = f2_pack(p0.z, p0.w);
+            const f2_t zj = f2_pack(p1.x, p1.y);
+            const f2_t mj = f2_pack(p1.z, p1.w);
+#pragma unroll
+            for (int g = 0; g < 2; ++g)
+                pair2<CLAMP>(xj, yj, zj, mj, xi[g], yi[g], zi[g], eps2, ax[g], ay[g], az[g]);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+            f2_two_sum(hx[g], lx[g], ax[g]);
+            f2_two_sum(hy[g], ly[g], ay[g]);
+            f2_two_sum(hz[g], lz[g], az[g]);
+        }
+    }
+    if (ok && cur_ib >= 0) flush(cur_ib);
+}
+
+size_t mixed_smem_bytes() { return (size_t)kStages * kTileBytes + 2 * kStages * sizeof(uint64_t); }
+
+}  // namespace
+
+nbg_status direct_fcompute(nbg_engine* e, const double* y, double* f) {
+    const int n = (int)e->count;
+    if (e->params.precision == NBG_PREC_FP64) {
+        ProfScope ps(e, NBG_K_DIRECT);
+        direct_fp64_kernel<<<(n + kF64Threads - 1) / kF64Threads, kF64Threads, 0, e->stream>>>(
+            y, e->d_mass, f, n);
+        NBG_LAUNCHED(e, "direct_fp64_kernel");
+        return NBG_OK;
+    }
+
+    // ---- mixed precision ----
+    const int n_jt = (n + kT - 1) / kT;
+    const int n_pad = n_jt * kT;
+    const size_t need = (size_t)n_pad * sizeof(Body2);
+    if (e->xyzm_cap < need) {
+        cudaFree(e->d_xyzm);
+        e->d_xyzm = nullptr;
+        e->xyzm_cap = 0;
+        NBG_CUDA(e, cudaMalloc(&e->d_xyzm, need));
+        e->xyzm_cap = need;
+    }
+    Body2* bodies = reinterpret_cast<Body2*>(e->d_xyzm);
+    pack_mixed_kernel<<<grid_for(n_pad, 256, (unsigned)e->sm_count * 8u), 256, 0, e->stream>>>(
+        y, e->d_mass, bodies, f, n, n_pad);
+    NBG_LAUNCHED(e, "pack_mixed_kernel");
+
+    const bool clamp = !(e->params.softening > 0.0);
+    const size_t smem = mixed_smem_bytes();
+    auto kern = clamp ? direct_mixed_kernel<true> : direct_mixed_kernel<false>;
+    const unsigned flag = clamp ? 1u : 2u;
+    if ((e->attr_flags & flag) == 0) {
+        NBG_CUDA(e, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem));
+        e->attr_flags |= flag;
+    }
+    int occ = 0;
+    NBG_CUDA(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreadsMixed, smem));
+    if (occ < 1) occ = 1;
+    MixedArgs a;
+    a.bodies = bodies;
+    a.acc = f + 3 * (size_t)n;
+    a.n = n;
+    a.n_jt = n_jt;
+    const long long n_ib = (n + kIB - 1) / kIB;
+    a.units = n_ib * n_jt;
+    a.eps2 = (float)(e->params.softening * e->params.softening);
+    a.err = e->d_err;
+    long long grid = (long long)e->sm_count * occ;
+    if (grid > a.units) grid = a.units;
+    ProfScope ps(e, NBG_K_DIRECT);
+    kern<<<(unsigned)grid, kThreadsMixed, smem, e->stream>>>(a);
+    NBG_LAUNCHED(e, "direct_mixed_kernel");
+    return NBG_OK;
+}
+
+}  // namespace nbg
