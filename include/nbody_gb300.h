@@ -167,6 +167,13 @@ nbg_status nbg_profile_query(nbg_engine* e, int kernel_id, double* total_ms,
 /* Number of kernels this engine has launched since creation. */
 uint64_t nbg_launch_count(const nbg_engine* e);
 
+/* Tuning knobs (set by the autotuner or by hand; no reference counterpart).
+ * Keys: "direct.pairs_per_lane" (2 or 4 packed i-pairs per lane),
+ *       "direct.unroll" (2, 4 or 8: j-loop unroll),
+ *       "direct.blocks_per_sm" (CTAs per SM of the persistent direct grid). */
+nbg_status nbg_tune_set(nbg_engine* e, const char* key, int64_t value);
+nbg_status nbg_tune_get(nbg_engine* e, const char* key, int64_t* value);
+
 /* FP32 FFMA throughput probe: runs a dependent-chain FMA kernel on the
  * engine's device and returns the measured FP32 FLOP/s (2 per FMA). */
 nbg_status nbg_measure_fp32_peak(nbg_engine* e, double* flops);

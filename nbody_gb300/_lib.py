@@ -31,7 +31,7 @@ EXPORTS = [
     "nbg_fmadd", "nbg_fmaddn_inplace", "nbg_fmaddn_corr", "nbg_fmaddn", "nbg_fmaxabs",
     "nbg_synchronize", "nbg_stream", "nbg_host_alloc", "nbg_host_free",
     "nbg_profile_enable", "nbg_profile_query", "nbg_launch_count",
-    "nbg_measure_fp32_peak",
+    "nbg_measure_fp32_peak", "nbg_tune_set", "nbg_tune_get",
 ]
 
 
@@ -114,5 +114,7 @@ def load() -> C.CDLL:
     _proto(lib, "nbg_profile_query", i32, vp, i32, dp, C.POINTER(u64))
     _proto(lib, "nbg_launch_count", u64, vp)
     _proto(lib, "nbg_measure_fp32_peak", i32, vp, dp)
+    _proto(lib, "nbg_tune_set", i32, vp, C.c_char_p, C.c_int64)
+    _proto(lib, "nbg_tune_get", i32, vp, C.c_char_p, C.POINTER(C.c_int64))
     _lib = lib
     return lib

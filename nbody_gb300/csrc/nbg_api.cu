@@ -647,6 +647,20 @@ nbg_status nbg_profile_query(nbg_engine* e, int kernel_id, double* total_ms,
 
 uint64_t nbg_launch_count(const nbg_engine* e) { return e == nullptr ? 0 : e->launches; }
 
+nbg_status nbg_tune_set(nbg_engine* e, const char* key, int64_t value) {
+    if (e == nullptr || key == nullptr) return NBG_ERR_INVALID_ARG;
+    e->tune[key] = value;
+    return NBG_OK;
+}
+
+nbg_status nbg_tune_get(nbg_engine* e, const char* key, int64_t* value) {
+    if (e == nullptr || key == nullptr || value == nullptr) return NBG_ERR_INVALID_ARG;
+    auto it = e->tune.find(key);
+    if (it == e->tune.end()) return set_error(e, NBG_ERR_INVALID_ARG, "tuning key %s not set", key);
+    *value = it->second;
+    return NBG_OK;
+}
+
 nbg_status nbg_measure_fp32_peak(nbg_engine* e, double* flops) {
     if (e == nullptr || flops == nullptr) return NBG_ERR_INVALID_ARG;
     return measure_fp32_peak(e, flops);

@@ -12,9 +12,10 @@
 //    A pack kernel turns y into a tile-padded array of bodies in
 //    (x x y y | z z m m) form and writes f = [v ; 0].  The force kernel is
 //    persistent: the (i-block, j-tile) units are split evenly over one wave
-//    of CTAs (stream-K), a producer warp streams j-tiles global -> shared with
-//    1-D bulk async copies (TMA) through an mbarrier ring, and 4 consumer
-//    warps each hold 4 i-bodies per lane in packed FP32x2 registers.  Per
+//    of CTAs (stream-K), thread 0 streams j-tiles global -> shared with 1-D
+//    bulk async copies (TMA) through a 4-stage mbarrier ring, and the 4 warps
+//    each hold 2G i-bodies per lane (G = 2 or 4 packed pairs) in FP32x2
+//    registers.  Per
 //    tile the FP32 partial sums are folded into a (hi, lo) two-sum pair; at
 //    the end of an i-block segment hi + lo is added into the FP64 a-part of f
 //    with one atomicAdd per component.  Pair term:
@@ -80,10 +81,9 @@ direct_fp64_kernel(const double* __restrict__ y, const double* __restrict__ mass
 // ---------------------------------------------------------------------------
 // mixed kernel
 // ---------------------------------------------------------------------------
-constexpr int kWarps = 4;                      // consumer warps per CTA
-constexpr int kThreadsMixed = (kWarps + 1) * 32;  // + one producer warp
-constexpr int kR = 4;                          // i-bodies per lane (2 packed pairs)
-constexpr int kIB = kWarps * 32 * kR;          // 512 i-bodies per i-block
+constexpr int kWarps = 4;                      // warps per CTA (all compute)
+constexpr int kThreadsMixed = kWarps * 32;
+constexpr int kMinBlocksMixed = 6;             // resident CTAs per SM targeted
 constexpr int kT = 128;                        // j-bodies per tile
 constexpr int kStages = 4;                     // tiles in flight
 constexpr uint32_t kTileBytes = kT * 32;       // 32 bytes per body (x x y y z z m m)
@@ -152,13 +152,31 @@ __device__ __forceinline__ void pair2(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f2_t x
     az = f2_fma(dz, s3, az);
 }
 
-template <bool CLAMP>
-__global__ void __launch_bounds__(kThreadsMixed)
+// Issue the bulk copy of j-tile `jt` into stage `s` (one thread).
+__device__ __forceinline__ void issue_tile(Body2* tiles, uint64_t* full, int s, int jt,
+                                           const Body2* bodies) {
+    mbar_arrive_expect_tx(&full[s], kTileBytes);
+    bulk_g2s(tiles + s * kT, bodies + (size_t)jt * kT, kTileBytes, &full[s]);
+}
+
+// G packed pairs (2G i-bodies) per lane; the j loop is unrolled UNR times.
+// i-body of lane `lane`, warp `warp`, slot r in [0, 2G):
+//     i = ib * IB + r * 128 + warp * 32 + lane,   IB = 128 * 2G,
+// so every slot is a coalesced row of 128 consecutive bodies.
+template <bool CLAMP, int G, int UNR>
+__global__ void __launch_bounds__(kThreadsMixed, G >= 4 ? 4 : kMinBlocksMixed)
 direct_mixed_kernel(MixedArgs a) {
+    constexpr int kIB = kThreadsMixed * 2 * G;
+    constexpr int kSlots = 6 * G;  // (hi, lo) x 3 components x G pairs
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Body2* tiles = reinterpret_cast<Body2*>(smem_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + kStages * kTileBytes);
     uint64_t* empty = full + kStages;
+    // Compensated per-body accumulators (hi, lo) live in shared memory: they
+    // are touched once per tile, and keeping them out of registers lets more
+    // CTAs stay resident.  Slot q = 2 * (3 * g + c) + {0: hi, 1: lo}.
+    f2_t* acc_sm = reinterpret_cast<f2_t*>(smem_raw + kStages * kTileBytes +
+                                           2 * kStages * sizeof(uint64_t));
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -166,8 +184,11 @@ direct_mixed_kernel(MixedArgs a) {
     const long long rem = a.units % gridDim.x;
     const long long u0 = blockIdx.x * per + min((long long)blockIdx.x, rem);
     const long long u1 = u0 + per + ((long long)blockIdx.x < rem ? 1 : 0);
+    const long long cnt = u1 - u0;
+    const bool producer = threadIdx.x == 0;
+    auto acc_at = [&](int q) -> f2_t& { return acc_sm[q * kThreadsMixed + threadIdx.x]; };
 
-    if (threadIdx.x == 0) {
+    if (producer) {
         for (int s = 0; s < kStages; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], kWarps);
@@ -175,108 +196,120 @@ direct_mixed_kernel(MixedArgs a) {
         mbar_fence_init();
     }
     __syncthreads();
-
-    if (warp == kWarps) {
-        // ---------------- producer warp: one lane issues the bulk copies ------
-        if (lane == 0) {
-            long long k = 0;
-            for (long long u = u0; u < u1; ++u, ++k) {
-                const int s = (int)(k % kStages);
-                const long long round = k / kStages;
-                if (round > 0 && !mbar_wait(&empty[s], (uint32_t)((round - 1) & 1), a.err)) break;
-                const int jt = (int)(u % a.n_jt);
-                mbar_arrive_expect_tx(&full[s], kTileBytes);
-                bulk_g2s(tiles + s * kT, a.bodies + (size_t)jt * kT, kTileBytes, &full[s]);
-            }
-        }
-        return;
+    if (producer) {  // prologue: fill the ring
+        for (long long k = 0; k < kStages && k < cnt; ++k)
+            issue_tile(tiles, full, (int)k, (int)((u0 + k) % a.n_jt), a.bodies);
     }
 
-    // -------------------- consumer warps ---------------------------------------
     const f2_t eps2 = f2_pack(a.eps2, a.eps2);
     const f2_t zero = f2_pack(0.f, 0.f);
-    f2_t xi[2], yi[2], zi[2];
-    f2_t hx[2], hy[2], hz[2], lx[2], ly[2], lz[2];
+    f2_t xi[G], yi[G], zi[G];
     long long cur_ib = -1;
-    long long k = 0;
     bool ok = true;
+    const uint32_t tiles_addr = smem_addr(tiles);
 
     auto flush = [&](long long ib) {
 #pragma unroll
-        for (int g = 0; g < 2; ++g) {
+        for (int g = 0; g < G; ++g) {
             float h0, h1, l0, l1;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const f2_t hh = c == 0 ? hx[g] : (c == 1 ? hy[g] : hz[g]);
-                const f2_t ll = c == 0 ? lx[g] : (c == 1 ? ly[g] : lz[g]);
-                f2_unpack(hh, h0, h1);
-                f2_unpack(ll, l0, l1);
-                const int i0 = (int)(ib * kIB) + (2 * g) * (kWarps * 32) + warp * 32 + lane;
-                const int i1 = i0 + kWarps * 32;
+                f2_unpack(acc_at(2 * (3 * g + c)), h0, h1);
+                f2_unpack(acc_at(2 * (3 * g + c) + 1), l0, l1);
+                const int i0 = (int)(ib * kIB) + (2 * g) * kThreadsMixed + warp * 32 + lane;
+                const int i1 = i0 + kThreadsMixed;
                 if (i0 < a.n) atomicAdd(a.acc + (size_t)c * a.n + i0, (double)h0 + (double)l0);
                 if (i1 < a.n) atomicAdd(a.acc + (size_t)c * a.n + i1, (double)h1 + (double)l1);
             }
         }
     };
 
-    for (long long u = u0; u < u1; ++u, ++k) {
+    for (long long k = 0; k < cnt; ++k) {
+        const long long u = u0 + k;
+        // Refill the stage that iteration k-1 freed, once every warp is done with it.
+        if (producer && k >= 1 && k - 1 + kStages < cnt) {
+            const int sp = (int)((k - 1) % kStages);
+            const uint32_t par = (uint32_t)(((k - 1) / kStages) & 1);
+            if (!mbar_wait(&empty[sp], par, a.err)) {
+                ok = false;
+                break;
+            }
+            issue_tile(tiles, full, sp, (int)((u - 1 + kStages) % a.n_jt), a.bodies);
+        }
         const long long ib = u / a.n_jt;
         if (ib != cur_ib) {
             if (cur_ib >= 0) flush(cur_ib);
             cur_ib = ib;
 #pragma unroll
-            for (int g = 0; g < 2; ++g) {
-                const int i0 = (int)(ib * kIB) + (2 * g) * (kWarps * 32) + warp * 32 + lane;
-                const int i1 = i0 + kWarps * 32;
+            for (int g = 0; g < G; ++g) {
+                const int i0 = (int)(ib * kIB) + (2 * g) * kThreadsMixed + warp * 32 + lane;
+                const int i1 = i0 + kThreadsMixed;
                 float x0 = 0.f, y0 = 0.f, z0 = 0.f, x1 = 0.f, y1 = 0.f, z1 = 0.f;
                 if (i0 < a.n) {
-                    const Body2 b = a.bodies[i0];
-                    x0 = b.xxyy.x; y0 = b.xxyy.z; z0 = b.zzmm.x;
+                    const float4 b = __ldg(&a.bodies[i0].xxyy);
+                    x0 = b.x; y0 = b.z; z0 = __ldg(&a.bodies[i0].zzmm.x);
                 }
                 if (i1 < a.n) {
-                    const Body2 b = a.bodies[i1];
-                    x1 = b.xxyy.x; y1 = b.xxyy.z; z1 = b.zzmm.x;
+                    const float4 b = __ldg(&a.bodies[i1].xxyy);
+                    x1 = b.x; y1 = b.z; z1 = __ldg(&a.bodies[i1].zzmm.x);
                 }
                 xi[g] = f2_pack(x0, x1);
                 yi[g] = f2_pack(y0, y1);
                 zi[g] = f2_pack(z0, z1);
-                hx[g] = hy[g] = hz[g] = zero;
-                lx[g] = ly[g] = lz[g] = zero;
             }
+#pragma unroll
+            for (int q = 0; q < kSlots; ++q) acc_at(q) = zero;
         }
         const int s = (int)(k % kStages);
-        const long long round = k / kStages;
-        if (!mbar_wait(&full[s], (uint32_t)(round & 1), a.err)) {
+        if (!mbar_wait(&full[s], (uint32_t)((k / kStages) & 1), a.err)) {
             ok = false;
             break;
         }
-        const Body2* tile = tiles + s * kT;
-        f2_t ax[2] = {zero, zero}, ay[2] = {zero, zero}, az[2] = {zero, zero};
-#pragma unroll 4
+        const uint32_t tbase = tiles_addr + (uint32_t)s * kTileBytes;
+        f2_t ax[G], ay[G], az[G];
+#pragma unroll
+        for (int g = 0; g < G; ++g) ax[g] = ay[g] = az[g] = zero;
+#pragma unroll UNR
         for (int j = 0; j < kT; ++j) {
-            const float4 p0 = tile[j].xxyy;
-            const float4 p1 = tile[j].zzmm;
+            const float4 p0 = lds128(tbase + 32u * j);
+            const float4 p1 = lds128(tbase + 32u * j + 16u);
             const f2_t xj = f2_pack(p0.x, p0.y);
             const f2_t yj = f2_pack(p0.z, p0.w);
             const f2_t zj = f2_pack(p1.x, p1.y);
             const f2_t mj = f2_pack(p1.z, p1.w);
 #pragma unroll
-            for (int g = 0; g < 2; ++g)
+            for (int g = 0; g < G; ++g)
                 pair2<CLAMP>(xj, yj, zj, mj, xi[g], yi[g], zi[g], eps2, ax[g], ay[g], az[g]);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);
 #pragma unroll
-        for (int g = 0; g < 2; ++g) {
-            f2_two_sum(hx[g], lx[g], ax[g]);
-            f2_two_sum(hy[g], ly[g], ay[g]);
-            f2_two_sum(hz[g], lz[g], az[g]);
+        for (int g = 0; g < G; ++g) {
+            f2_two_sum(acc_at(2 * (3 * g + 0)), acc_at(2 * (3 * g + 0) + 1), ax[g]);
+            f2_two_sum(acc_at(2 * (3 * g + 1)), acc_at(2 * (3 * g + 1) + 1), ay[g]);
+            f2_two_sum(acc_at(2 * (3 * g + 2)), acc_at(2 * (3 * g + 2) + 1), az[g]);
         }
     }
     if (ok && cur_ib >= 0) flush(cur_ib);
 }
 
-size_t mixed_smem_bytes() { return (size_t)kStages * kTileBytes + 2 * kStages * sizeof(uint64_t); }
+size_t mixed_smem_bytes(int G) {
+    return (size_t)kStages * kTileBytes + 2 * kStages * sizeof(uint64_t) +
+           6 * G * kThreadsMixed * sizeof(f2_t);
+}
+
+using MixedKernel = void (*)(MixedArgs);
+
+template <bool CLAMP>
+MixedKernel pick_mixed(int G, int unr) {
+    if (G == 4) {
+        if (unr <= 2) return direct_mixed_kernel<CLAMP, 4, 2>;
+        return direct_mixed_kernel<CLAMP, 4, 4>;
+    }
+    if (unr <= 2) return direct_mixed_kernel<CLAMP, 2, 2>;
+    if (unr >= 8) return direct_mixed_kernel<CLAMP, 2, 8>;
+    return direct_mixed_kernel<CLAMP, 2, 4>;
+}
 
 }  // namespace
 
@@ -307,23 +340,24 @@ nbg_status direct_fcompute(nbg_engine* e, const double* y, double* f) {
     NBG_LAUNCHED(e, "pack_mixed_kernel");
 
     const bool clamp = !(e->params.softening > 0.0);
-    const size_t smem = mixed_smem_bytes();
-    auto kern = clamp ? direct_mixed_kernel<true> : direct_mixed_kernel<false>;
-    const unsigned flag = clamp ? 1u : 2u;
-    if ((e->attr_flags & flag) == 0) {
-        NBG_CUDA(e, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem));
-        e->attr_flags |= flag;
-    }
+    const int G = e->tune_get("direct.pairs_per_lane", 4) >= 4 ? 4 : 2;
+    const int unr = (int)e->tune_get("direct.unroll", 4);
+    MixedKernel kern = clamp ? pick_mixed<true>(G, unr) : pick_mixed<false>(G, unr);
+    const size_t smem = mixed_smem_bytes(G);
+    NBG_CUDA(e, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
     int occ = 0;
     NBG_CUDA(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreadsMixed, smem));
     if (occ < 1) occ = 1;
+    const int64_t bps = e->tune_get("direct.blocks_per_sm", 0);
+    if (bps > 0 && bps < occ) occ = (int)bps;
     MixedArgs a;
     a.bodies = bodies;
     a.acc = f + 3 * (size_t)n;
     a.n = n;
     a.n_jt = n_jt;
-    const long long n_ib = (n + kIB - 1) / kIB;
+    const int ib_size = kThreadsMixed * 2 * G;
+    const long long n_ib = (n + ib_size - 1) / ib_size;
     a.units = n_ib * n_jt;
     a.eps2 = (float)(e->params.softening * e->params.softening);
     a.err = e->d_err;

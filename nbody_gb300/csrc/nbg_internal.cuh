@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <cstdio>
+#include <map>
 #include <string>
 #include <unordered_set>
 #include <vector>
@@ -72,7 +73,11 @@ struct nbg_engine {
     } prof[NBG_K_COUNT];
     std::vector<cudaEvent_t> event_pool;
     uint64_t launches = 0;
-    unsigned attr_flags = 0;  // kernels whose smem attribute is set on this device
+    std::map<std::string, int64_t> tune;  // autotuner knobs
+    int64_t tune_get(const char* key, int64_t dflt) const {
+        auto it = tune.find(key);
+        return it == tune.end() ? dflt : it->second;
+    }
 };
 
 namespace nbg {

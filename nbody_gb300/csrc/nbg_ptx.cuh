@@ -86,6 +86,15 @@ __device__ __forceinline__ void bulk_g2s(void* dst_smem, const void* src_gmem, u
         : "memory");
 }
 
+// ---- shared-memory vector load (forces LDS.128 on a 32-bit shared address) ----
+__device__ __forceinline__ float4 lds128(uint32_t addr) {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(addr));
+    return v;
+}
+
 // ---- packed FP32x2 arithmetic (sm_100+) -------------------------------------
 typedef unsigned long long f2_t;  // two floats in one 64-bit register pair
 

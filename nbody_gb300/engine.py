@@ -421,6 +421,14 @@ class NbodyEngineGB300:
         self._check(self._lib.nbg_measure_fp32_peak(self._h, C.byref(r)), "measure_fp32_peak")
         return r.value
 
+    def tune_set(self, key: str, value: int) -> None:
+        self._check(self._lib.nbg_tune_set(self._h, key.encode(), int(value)), "tune_set")
+
+    def tune_get(self, key: str):
+        v = C.c_int64(0)
+        st = self._lib.nbg_tune_get(self._h, key.encode(), C.byref(v))
+        return v.value if st == 0 else None
+
     @property
     def handle(self) -> int:
         return self._h
