@@ -39,7 +39,8 @@ typedef enum nbg_status {
     NBG_ERR_UNSUPPORTED = 6,     /* e.g. Barnes-Hut with N not a power of two */
     NBG_ERR_NOT_INITIALIZED = 7, /* nbg_init has not been called */
     NBG_ERR_DEVICE_TIMEOUT = 8,  /* a bounded device-side wait gave up */
-    NBG_ERR_DEVICE_ERROR = 9     /* a kernel reported an error flag */
+    NBG_ERR_DEVICE_ERROR = 9,    /* a kernel reported an error flag */
+    NBG_ERR_TOO_LARGE = 10       /* request exceeds a fixed, preallocated capacity */
 } nbg_status;
 
 typedef struct nbg_engine nbg_engine; /* opaque engine */
@@ -173,6 +174,27 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       "direct.blocks_per_sm" (CTAs per SM of the persistent direct grid). */
 nbg_status nbg_tune_set(nbg_engine* e, const char* key, int64_t value);
 nbg_status nbg_tune_get(nbg_engine* e, const char* key, int64_t* value);
+
+/* ---- allocation-free direct sum (no counterpart in the reference) ----
+ * For callers that must not allocate GPU memory -- e.g. a host application
+ * that hands out all device memory from its own arena, or a time-critical
+ * loop where an allocation and its implicit device synchronisation are not
+ * allowed.  Computes f = [v ; a(y)] for n bodies with the mixed-precision
+ * direct sum (FP32 pairs, compensated sums, FP64 in and out; softening >= 0,
+ * 0 = the reference clamp r^2 >= 1e-8), exactly like nbg_fcompute of a
+ * mixed-precision direct engine.  y (6n doubles), mass (n) and f (6n) are
+ * device pointers on the current device; stream is a cudaStream_t (NULL =
+ * the default stream).  It calls no allocator: the kernel's packed-body
+ * scratch is a fixed array compiled into the library, present on every GPU
+ * that loads it until the process exits, which caps n at
+ * NBG_NOALLOC_MAX_BODIES (larger n returns NBG_ERR_TOO_LARGE and touches
+ * nothing).  The first call on a device looks up that array's device address
+ * (one-time set-up, with that device current).  Returns after f holds the
+ * result.  All calls share the one array: calls that overlap on the GPU
+ * (from several host threads or streams) race and must be serialised. */
+#define NBG_NOALLOC_MAX_BODIES 131072
+nbg_status nbg_direct_mixed_noalloc(const double* y, const double* mass, double* f,
+                                    size_t n, double softening, void* stream);
 
 /* FP32 FFMA throughput probe: runs a dependent-chain FMA kernel on the
  * engine's device and returns the measured FP32 FLOP/s (2 per FMA). */

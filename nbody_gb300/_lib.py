@@ -14,7 +14,8 @@ LIB_PATH = Path(__file__).resolve().parent / "libnbody_gb300.so"
 NBG_OK = 0
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "foreign buffer", 3: "size mismatch",
                 4: "out of memory", 5: "cuda error", 6: "unsupported",
-                7: "not initialized", 8: "device timeout", 9: "device error"}
+                7: "not initialized", 8: "device timeout", 9: "device error",
+                10: "exceeds a fixed capacity"}
 ALGO = {"direct": 0, "bh": 1}
 PRECISION = {"fp64": 0, "mixed": 1}
 LAYOUT = {"heap": 1, "heap_stackless": 2}
@@ -31,7 +32,7 @@ EXPORTS = [
     "nbg_fmadd", "nbg_fmaddn_inplace", "nbg_fmaddn_corr", "nbg_fmaddn", "nbg_fmaxabs",
     "nbg_synchronize", "nbg_stream", "nbg_host_alloc", "nbg_host_free",
     "nbg_profile_enable", "nbg_profile_query", "nbg_launch_count",
-    "nbg_measure_fp32_peak", "nbg_tune_set", "nbg_tune_get",
+    "nbg_measure_fp32_peak", "nbg_tune_set", "nbg_tune_get", "nbg_direct_mixed_noalloc",
 ]
 
 
@@ -116,5 +117,6 @@ def load() -> C.CDLL:
     _proto(lib, "nbg_measure_fp32_peak", i32, vp, dp)
     _proto(lib, "nbg_tune_set", i32, vp, C.c_char_p, C.c_int64)
     _proto(lib, "nbg_tune_get", i32, vp, C.c_char_p, C.POINTER(C.c_int64))
+    _proto(lib, "nbg_direct_mixed_noalloc", i32, vp, vp, vp, sz, dbl, vp)
     _lib = lib
     return lib

@@ -166,6 +166,7 @@ const char* nbg_status_string(nbg_status s) {
         case NBG_ERR_NOT_INITIALIZED: return "not initialized";
         case NBG_ERR_DEVICE_TIMEOUT: return "device timeout";
         case NBG_ERR_DEVICE_ERROR: return "device error";
+        case NBG_ERR_TOO_LARGE: return "exceeds a fixed capacity";
     }
     return "unknown";
 }

@@ -21,6 +21,8 @@
 //    with one atomicAdd per component.  Pair term:
 //        a_i += m_j (r_j - r_i) / (|r_j - r_i|^2 + eps^2)^{3/2}
 //    with r^2 clamped to >= 1e-8 when eps = 0 (the reference clamp).
+#include <mutex>
+
 #include "nbg_internal.cuh"
 #include "nbg_ptx.cuh"
 
@@ -370,3 +372,119 @@ nbg_status direct_fcompute(nbg_engine* e, const double* y, double* f) {
 }
 
 }  // namespace nbg
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the mixed-precision direct sum
+// ---------------------------------------------------------------------------
+// Some callers cannot call cudaMalloc: a host application that owns all GPU
+// memory through its own arena and forbids allocations behind its back, or a
+// time-stepping loop with a hard latency budget where an allocation (and the
+// device synchronisation it implies) is not allowed.  For them the packed-body
+// scratch of the kernel above lives in a fixed file-scope device array instead
+// of an engine allocation.  The array is created with this module on every GPU
+// that loads the library and stays there until the process exits, so its size
+// is capped: NBG_NOALLOC_MAX_BODIES bodies x 32 bytes = 4 MiB, plus one error
+// word.
+namespace nbg {
+namespace {
+
+static __device__ __align__(256) Body2 g_noalloc_bodies[NBG_NOALLOC_MAX_BODIES];
+static __device__ __align__(256) unsigned g_noalloc_err;
+
+constexpr int kNoallocMaxDevices = 64;
+struct NoallocDevice {
+    bool ready;
+    Body2* bodies;  // device address of g_noalloc_bodies on this device
+    unsigned* err;  // device address of g_noalloc_err on this device
+    int sm_count;
+};
+std::mutex g_noalloc_mu;
+NoallocDevice g_noalloc_dev[kNoallocMaxDevices];
+
+}  // namespace
+}  // namespace nbg
+
+extern "C" nbg_status nbg_direct_mixed_noalloc(const double* y, const double* mass, double* f,
+                                               size_t n, double softening, void* stream) {
+    using namespace nbg;
+    if (y == nullptr || mass == nullptr || f == nullptr || n == 0 || !(softening >= 0.0))
+        return NBG_ERR_INVALID_ARG;
+    if (n > (size_t)NBG_NOALLOC_MAX_BODIES) return NBG_ERR_TOO_LARGE;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocMaxDevices)
+        return NBG_ERR_CUDA;
+
+    // One-time set-up per device, on the current device: host code cannot use
+    // the array's name as a device address, so look the address up.
+    NoallocDevice d;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        NoallocDevice& slot = g_noalloc_dev[dev];
+        if (!slot.ready) {
+            void* pb = nullptr;
+            void* pe = nullptr;
+            if (cudaGetSymbolAddress(&pb, g_noalloc_bodies) != cudaSuccess ||
+                cudaGetSymbolAddress(&pe, g_noalloc_err) != cudaSuccess ||
+                cudaDeviceGetAttribute(&slot.sm_count, cudaDevAttrMultiProcessorCount, dev) !=
+                    cudaSuccess) {
+                cudaGetLastError();
+                return NBG_ERR_CUDA;
+            }
+            slot.bodies = static_cast<Body2*>(pb);
+            slot.err = static_cast<unsigned*>(pe);
+            slot.ready = true;
+        }
+        d = slot;
+    }
+
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int nn = (int)n;
+    const int n_jt = (nn + kT - 1) / kT;
+    const int n_pad = n_jt * kT;
+    const bool clamp = !(softening > 0.0);
+    constexpr int G = 4;
+    MixedKernel kern = clamp ? pick_mixed<true>(G, 4) : pick_mixed<false>(G, 4);
+    const size_t smem = mixed_smem_bytes(G);
+    int occ = 0;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreadsMixed, smem) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        return NBG_ERR_CUDA;
+    }
+    if (occ < 1) occ = 1;
+
+    // The error word must start at zero; the pack kernel rewrites every
+    // scratch entry the force kernel reads (padding included) and zeroes the
+    // acceleration half of f, so nothing else carries over from earlier calls.
+    if (cudaMemsetAsync(d.err, 0, sizeof(unsigned), st) != cudaSuccess) {
+        cudaGetLastError();
+        return NBG_ERR_CUDA;
+    }
+    pack_mixed_kernel<<<grid_for(n_pad, 256, (unsigned)d.sm_count * 8u), 256, 0, st>>>(
+        y, mass, d.bodies, f, nn, n_pad);
+    MixedArgs a;
+    a.bodies = d.bodies;
+    a.acc = f + 3 * n;
+    a.n = nn;
+    a.n_jt = n_jt;
+    const long long n_ib = (nn + kThreadsMixed * 2 * G - 1) / (kThreadsMixed * 2 * G);
+    a.units = n_ib * n_jt;
+    a.eps2 = (float)(softening * softening);
+    a.err = d.err;
+    long long grid = (long long)d.sm_count * occ;
+    if (grid > a.units) grid = a.units;
+    kern<<<(unsigned)grid, kThreadsMixed, smem, st>>>(a);
+    if (cudaGetLastError() != cudaSuccess) return NBG_ERR_CUDA;
+
+    // Synchronous: the result is in f when this returns, and a device-side
+    // wait that timed out is reported here.
+    unsigned err_host = 0;
+    if (cudaStreamSynchronize(st) != cudaSuccess ||
+        cudaMemcpy(&err_host, d.err, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return NBG_ERR_CUDA;
+    }
+    return err_host != 0 ? NBG_ERR_DEVICE_TIMEOUT : NBG_OK;
+}

@@ -1,0 +1,79 @@
+"""The allocation-free direct sum, called through the C ABI, against the
+engine's own mixed-precision fcompute.
+
+nbg_direct_mixed_noalloc serves callers that may not allocate GPU memory (an
+application that owns all device memory through its own arena, or a loop that
+must not pay for an allocation and its device synchronisation); its scratch
+is a fixed array inside the library.  This file is collected last so that a
+run stopping at the first failure has already run every other test; it also
+passes on its own in a fresh process (the first call does the per-device
+set-up).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from nbody_gb300.data import NBodyData
+
+pytestmark = pytest.mark.gpu
+
+MAX_BODIES = 131072  # NBG_NOALLOC_MAX_BODIES in include/nbody_gb300.h
+RTOL = 1e-12         # same kernel; only the order of FP64 atomic adds may differ
+
+
+def _engine_reference(make_engine, d, eps):
+    """f from the existing entry point: a mixed-precision engine's fcompute."""
+    n = d.get_count()
+    e = make_engine(precision="mixed", softening=eps)
+    assert e.init(d)
+    f = e.create_buffer(8 * 6 * n)
+    e.fcompute(0.0, e.get_y(), f)
+    out = np.zeros(6 * n)
+    e.read_buffer(out, f)
+    return e, out
+
+
+def _noalloc(gpulib, e, d, eps):
+    """Run the allocation-free entry point on buffers the test owns."""
+    n = d.get_count()
+    y = e.create_buffer(8 * 6 * n)
+    m = e.create_buffer(8 * n)
+    f = e.create_buffer(8 * 6 * n)
+    e.write_buffer(y, d.to_state())
+    e.write_buffer(m, np.ascontiguousarray(d.mass, dtype=np.float64))
+    e.fill_buffer(f, 1e10)  # poison: every element must be written
+    e.synchronize()
+    st = gpulib.nbg_direct_mixed_noalloc(y.device_ptr(), m.device_ptr(), f.device_ptr(),
+                                         n, eps, gpulib.nbg_stream(e.handle))
+    assert st == 0, gpulib.nbg_status_string(st)
+    out = np.zeros(6 * n)
+    e.read_buffer(out, f)
+    return out
+
+
+@pytest.mark.parametrize("eps", [1e-3, 0.0])
+def test_noalloc_matches_fcompute_two_calls(make_engine, gpulib, eps):
+    # Two calls in a row on different systems; the second is smaller, so any
+    # stale scratch from the first call would show up in its result.
+    for n, seed in ((5003, 1), (1200, 2)):
+        d = NBodyData.plummer(n, seed=seed)
+        e, f_ref = _engine_reference(make_engine, d, eps)
+        f = _noalloc(gpulib, e, d, eps)
+        assert np.array_equal(f[:3 * n], f_ref[:3 * n])
+        a, a_ref = f[3 * n:], f_ref[3 * n:]
+        assert np.all(np.isfinite(a))
+        assert np.max(np.abs(a - a_ref)) <= RTOL * np.max(np.abs(a_ref))
+
+
+def test_noalloc_rejects_oversize(make_engine, gpulib):
+    d = NBodyData.uniform_cube(64, seed=3)
+    e = make_engine(precision="mixed", softening=1e-3)
+    assert e.init(d)
+    big = MAX_BODIES + 1
+    y = e.create_buffer(8 * 6 * 64)
+    st = gpulib.nbg_direct_mixed_noalloc(y.device_ptr(), y.device_ptr(), y.device_ptr(),
+                                         big, 1e-3, None)
+    assert st == 10  # NBG_ERR_TOO_LARGE, nothing launched
+    assert gpulib.nbg_status_string(st) == b"exceeds a fixed capacity"
+    assert gpulib.nbg_direct_mixed_noalloc(None, None, None, 16, 1e-3, None) == 1
