@@ -165,6 +165,10 @@ nbg_status nbg_profile_enable(nbg_engine* e, int enable);
 /* Accumulated device time (ms) and launches of one kernel class; resets it. */
 nbg_status nbg_profile_query(nbg_engine* e, int kernel_id, double* total_ms,
                              uint64_t* launches);
+/* Barnes-Hut walk counters since the last call (mixed walk): node visits
+ * (per warp: every visit is one broadcast node load) and accepted
+ * body-node interactions; resets them. */
+nbg_status nbg_bh_counters(nbg_engine* e, uint64_t* visits, uint64_t* interactions);
 /* Number of kernels this engine has launched since creation. */
 uint64_t nbg_launch_count(const nbg_engine* e);
 

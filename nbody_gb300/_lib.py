@@ -33,6 +33,7 @@ EXPORTS = [
     "nbg_synchronize", "nbg_stream", "nbg_host_alloc", "nbg_host_free",
     "nbg_profile_enable", "nbg_profile_query", "nbg_launch_count",
     "nbg_measure_fp32_peak", "nbg_tune_set", "nbg_tune_get", "nbg_direct_mixed_noalloc",
+    "nbg_bh_counters",
 ]
 
 
@@ -118,5 +119,6 @@ def load() -> C.CDLL:
     _proto(lib, "nbg_tune_set", i32, vp, C.c_char_p, C.c_int64)
     _proto(lib, "nbg_tune_get", i32, vp, C.c_char_p, C.POINTER(C.c_int64))
     _proto(lib, "nbg_direct_mixed_noalloc", i32, vp, vp, vp, sz, dbl, vp)
+    _proto(lib, "nbg_bh_counters", i32, vp, C.POINTER(u64), C.POINTER(u64))
     _lib = lib
     return lib

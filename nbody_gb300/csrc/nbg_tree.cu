@@ -1,0 +1,492 @@
+// nbg_tree.cu -- GPU build of the reference's kd-median heap.
+//
+// The reference builds the tree on the host (nbody/nbody_space_heap.cpp:13-37,
+// 136-190): recursive median split with std::nth_element along x, y, z in
+// turn; the left child takes the count/2 smallest bodies; then a bottom-up
+// update of mass, mass centre, bounding box and the critical radius
+// (nbody/nbody_space_heap.cpp:119-134).
+//
+// GPU form (N = 2^K bodies):
+//  1. Three stable LSD radix sorts of the bodies by x, y and z with exact
+//     FP64 keys (ties broken by body index) give three lists.
+//  2. Level by level (segment size S = N >> level, split axis = level mod 3)
+//     the list of the split axis is already ordered inside every segment, so
+//     its first S/2 entries are exactly the left child.  A flag per body marks
+//     them; the two other lists are stably partitioned by that flag, which
+//     keeps every child segment ordered along all three axes.  After K levels
+//     the lists give the leaf order: leaf N + p holds body list[p].
+//  3. Bottom-up, one launch per level, the reference's node update in FP64
+//     with explicit roundings (no contraction), so nodes match a
+//     non-contracting build of the reference bit for bit.
+// With distinct coordinates the subsets equal nth_element's; the whole tree,
+// and therefore every acceptance decision of the walk, matches the reference.
+#include <cstring>
+
+#include "nbg_tree.cuh"
+
+namespace nbg {
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;  // 2048 keys per block
+constexpr int kDigits = 256;
+
+__device__ __forceinline__ uint64_t order_key(double v) {
+    const uint64_t b = (uint64_t)__double_as_longlong(v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void init_keys_kernel(const double* __restrict__ coord, int n,
+                                 uint64_t* __restrict__ keys, int* __restrict__ vals) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        keys[i] = order_key(coord[i]);
+        vals[i] = i;
+    }
+}
+
+// Per-block digit histogram: hist[digit * nblocks + block].
+__global__ void __launch_bounds__(kSortThreads)
+radix_hist_kernel(const uint64_t* __restrict__ keys, int n, int shift, unsigned* __restrict__ hist) {
+    __shared__ unsigned h[kDigits];
+    for (int d = threadIdx.x; d < kDigits; d += kSortThreads) h[d] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile;
+    for (int k = threadIdx.x; k < kSortTile; k += kSortThreads) {
+        const int i = base + k;
+        if (i < n) atomicAdd(&h[(unsigned)(keys[i] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kDigits; d += kSortThreads) hist[d * gridDim.x + blockIdx.x] = h[d];
+}
+
+// Exclusive scan of hist in (digit, block) order, in place; one CTA.
+__global__ void __launch_bounds__(1024) radix_scan_kernel(unsigned* __restrict__ hist, int count) {
+    __shared__ unsigned partial[1024];
+    const int per = (count + 1023) / 1024;
+    const int b0 = threadIdx.x * per;
+    unsigned s = 0;
+    for (int k = 0; k < per; ++k)
+        if (b0 + k < count) s += hist[b0 + k];
+    partial[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {  // Hillis-Steele inclusive scan
+        unsigned v = threadIdx.x >= off ? partial[threadIdx.x - off] : 0u;
+        __syncthreads();
+        partial[threadIdx.x] += v;
+        __syncthreads();
+    }
+    unsigned run = threadIdx.x ? partial[threadIdx.x - 1] : 0u;
+    for (int k = 0; k < per; ++k)
+        if (b0 + k < count) {
+            unsigned v = hist[b0 + k];
+            hist[b0 + k] = run;
+            run += v;
+        }
+}
+
+// Stable scatter.  Each warp owns 256 consecutive keys of the tile and walks
+// them in 8 rounds of 32; __match_any_sync ranks equal digits inside a round,
+// per-warp digit counters carry the rank across rounds, and a per-digit
+// prefix over the warps orders the warps.  Order inside the tile is kept.
+__global__ void __launch_bounds__(kSortThreads)
+radix_scatter_kernel(const uint64_t* __restrict__ kin, const int* __restrict__ vin,
+                     uint64_t* __restrict__ kout, int* __restrict__ vout, int n, int shift,
+                     const unsigned* __restrict__ offsets) {
+    constexpr int kWarpsS = kSortThreads / 32;
+    __shared__ unsigned cnt[kWarpsS][kDigits];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int d = lane; d < kDigits; d += 32) cnt[warp][d] = 0;
+    __syncwarp();
+    const int base = blockIdx.x * kSortTile + warp * (32 * kSortItems);
+    const unsigned lt = (1u << lane) - 1u;
+    uint64_t key[kSortItems];
+    int val[kSortItems];
+    unsigned rank[kSortItems];
+    unsigned dig[kSortItems];
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int i = base + r * 32 + lane;
+        const bool live = i < n;
+        key[r] = live ? kin[i] : 0ull;
+        val[r] = live ? vin[i] : 0;
+        dig[r] = live ? ((unsigned)(key[r] >> shift) & 0xFFu) : kDigits;  // kDigits = dead
+        const unsigned peers = __match_any_sync(0xffffffffu, dig[r]);
+        const unsigned before = __popc(peers & lt);
+        const int leader = __ffs(peers) - 1;
+        unsigned b = 0;
+        if (live) b = cnt[warp][dig[r]];
+        rank[r] = b + before;
+        __syncwarp();
+        if (live && lane == leader) cnt[warp][dig[r]] = b + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // per-digit prefix over warps (warp order = key order inside the tile)
+    for (int d = threadIdx.x; d < kDigits; d += kSortThreads) {
+        unsigned run = offsets[d * gridDim.x + blockIdx.x];
+        for (int w = 0; w < kWarpsS; ++w) {
+            const unsigned c = cnt[w][d];
+            cnt[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        if (dig[r] < (unsigned)kDigits) {
+            const unsigned dst = cnt[warp][dig[r]] + rank[r];
+            kout[dst] = key[r];
+            vout[dst] = val[r];
+        }
+    }
+}
+
+// flag[body] = 1 when the body is in the left half of its segment of the
+// split-axis list.
+__global__ void split_flag_kernel(const int* __restrict__ list, int n, int S,
+                                  unsigned char* __restrict__ flag) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        flag[list[p]] = (unsigned char)((p & (S - 1)) < (S >> 1));
+}
+
+struct PartArgs {
+    const int* in[2];
+    int* out[2];
+    const unsigned char* flag;
+    int* tile_count;  // [2][ntiles]
+    int ntiles;
+    int n;
+    int S;
+};
+
+__global__ void __launch_bounds__(256) part_count_kernel(PartArgs a) {
+    const int* in = a.in[blockIdx.y];
+    int c = 0;
+    const int base = blockIdx.x * kPartTile;
+    for (int k = threadIdx.x; k < kPartTile; k += 256) {
+        const int p = base + k;
+        if (p < a.n) c += a.flag[in[p]];
+    }
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    __shared__ int ws[8];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < 8; ++w) t += ws[w];
+        a.tile_count[blockIdx.y * a.ntiles + blockIdx.x] = t;
+    }
+}
+
+// Stable partition of each segment by flag: left entries keep their order in
+// [seg, seg + S/2), right entries in [seg + S/2, seg + S).
+__global__ void __launch_bounds__(256) part_scatter_kernel(PartArgs a) {
+    constexpr int kItems = kPartTile / 256;
+    __shared__ int excl[kPartTile];  // exclusive count of lefts before each tile slot
+    __shared__ int wsum[8];
+    __shared__ int seg_prefix;
+    const int* in = a.in[blockIdx.y];
+    int* out = a.out[blockIdx.y];
+    const int tile0 = blockIdx.x * kPartTile;
+    int body[kItems];
+    int fl[kItems];
+    int mine = 0;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const int p = tile0 + threadIdx.x * kItems + k;
+        body[k] = p < a.n ? in[p] : -1;
+        fl[k] = body[k] >= 0 ? a.flag[body[k]] : 0;
+        mine += fl[k];
+    }
+    // block exclusive scan of per-thread counts
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    int wbase = 0;
+    for (int w = 0; w < warp; ++w) wbase += wsum[w];
+    int run = wbase + incl - mine;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        excl[threadIdx.x * kItems + k] = run;
+        run += fl[k];
+    }
+    // lefts in earlier tiles of the same segment (segments longer than a tile)
+    if (threadIdx.x == 0) seg_prefix = 0;
+    __syncthreads();
+    if (a.S > kPartTile) {
+        const int seg_tile0 = (tile0 & ~(a.S - 1)) / kPartTile;
+        int s = 0;
+        for (int t = seg_tile0 + threadIdx.x; t < (int)blockIdx.x; t += 256)
+            s += a.tile_count[blockIdx.y * a.ntiles + t];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) atomicAdd(&seg_prefix, s);
+    }
+    __syncthreads();
+    const int half = a.S >> 1;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        if (body[k] < 0) continue;
+        const int slot = threadIdx.x * kItems + k;
+        const int p = tile0 + slot;
+        const int seg = p & ~(a.S - 1);
+        int left_before;
+        if (seg >= tile0)
+            left_before = excl[slot] - excl[seg - tile0];
+        else
+            left_before = seg_prefix + excl[slot];
+        const int dst = fl[k] ? seg + left_before : seg + half + ((p - seg) - left_before);
+        out[dst] = body[k];
+    }
+}
+
+// Leaves: leaf n + p holds body list[p] (nbody/nbody_space_heap.cpp:141-148).
+__global__ void leaf_init_kernel(const int* __restrict__ order, const double* __restrict__ y,
+                                 const double* __restrict__ mass, int n, TreeState t) {
+    const size_t sz = t.size;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const int b = order[p];
+        const size_t idx = (size_t)n + p;
+        t.body_n[idx] = b;
+        const double x = y[b], yy = y[n + b], z = y[2 * n + b];
+        t.com[idx] = x;
+        t.com[sz + idx] = yy;
+        t.com[2 * sz + idx] = z;
+        t.bmin[idx] = x;
+        t.bmin[sz + idx] = yy;
+        t.bmin[2 * sz + idx] = z;
+        t.bmax[idx] = x;
+        t.bmax[sz + idx] = yy;
+        t.bmax[2 * sz + idx] = z;
+        t.mass[idx] = mass[b];
+        t.crit2[idx] = 0.0;
+        t.node4[idx] = make_float4((float)x, (float)yy, (float)z, 0.f);
+        t.nodem[idx] = (float)mass[b];
+    }
+}
+
+// Refit leaves: new positions, same bodies (nbody/nbody_space_heap.cpp:45-53).
+__global__ void leaf_refit_kernel(const double* __restrict__ y, int n, TreeState t) {
+    const size_t sz = t.size;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const size_t idx = (size_t)n + p;
+        const int b = t.body_n[idx];
+        const double x = y[b], yy = y[n + b], z = y[2 * n + b];
+        t.com[idx] = x;
+        t.com[sz + idx] = yy;
+        t.com[2 * sz + idx] = z;
+        t.bmin[idx] = x;
+        t.bmin[sz + idx] = yy;
+        t.bmin[2 * sz + idx] = z;
+        t.bmax[idx] = x;
+        t.bmax[sz + idx] = yy;
+        t.bmax[2 * sz + idx] = z;
+        t.node4[idx] = make_float4((float)x, (float)yy, (float)z, 0.f);
+    }
+}
+
+__device__ __forceinline__ double len3(double x, double y, double z) {
+    return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
+}
+
+// One level of the bottom-up update (nbody/nbody_space_heap.cpp:119-134).
+__global__ void update_level_kernel(int first, int count, double lambda2, TreeState t) {
+    const size_t sz = t.size;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const size_t idx = (size_t)first + k;
+        const size_t l = 2 * idx, r = 2 * idx + 1;
+        const double ml = t.mass[l], mr = t.mass[r];
+        const double m = __dadd_rn(ml, mr);
+        double c[3], mn[3], mx[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            c[d] = __ddiv_rn(__dadd_rn(__dmul_rn(t.com[d * sz + l], ml), __dmul_rn(t.com[d * sz + r], mr)), m);
+            const double al = t.bmin[d * sz + l], ar = t.bmin[d * sz + r];
+            mn[d] = (ar < al) ? ar : al;  // std::min(left, right)
+            const double bl = t.bmax[d * sz + l], br = t.bmax[d * sz + r];
+            mx[d] = (bl < br) ? br : bl;  // std::max(left, right)
+            t.com[d * sz + idx] = c[d];
+            t.bmin[d * sz + idx] = mn[d];
+            t.bmax[d * sz + idx] = mx[d];
+        }
+        t.mass[idx] = m;
+        const double rr = __dadd_rn(
+            __dmul_rn(len3(__dsub_rn(mx[0], mn[0]), __dsub_rn(mx[1], mn[1]), __dsub_rn(mx[2], mn[2])), 0.5),
+            len3(__dsub_rn(__ddiv_rn(__dadd_rn(mx[0], mn[0]), 2.0), c[0]),
+                 __dsub_rn(__ddiv_rn(__dadd_rn(mx[1], mn[1]), 2.0), c[1]),
+                 __dsub_rn(__ddiv_rn(__dadd_rn(mx[2], mn[2]), 2.0), c[2])));
+        const double cr2 = __dmul_rn(__dmul_rn(rr, rr), lambda2);
+        t.crit2[idx] = cr2;
+        t.node4[idx] = make_float4((float)c[0], (float)c[1], (float)c[2], (float)cr2);
+        t.nodem[idx] = (float)m;
+    }
+}
+
+template <typename T>
+nbg_status alloc(nbg_engine* e, T** p, size_t count) {
+    NBG_CUDA(e, cudaMalloc(p, count * sizeof(T) + 256));
+    return NBG_OK;
+}
+
+nbg_status tree_alloc(nbg_engine* e) {
+    TreeState* t = e->tree;
+    const size_t n = t->n, sz = t->size;
+    const size_t ntiles = n / kPartTile + 1;
+    const size_t nblocks = n / kSortTile + 1;
+    nbg_status s = NBG_OK;
+#define NBG_TRY(x)               \
+    if ((s = (x)) != NBG_OK) return s;
+    NBG_TRY(alloc(e, &t->keys[0], n));
+    NBG_TRY(alloc(e, &t->keys[1], n));
+    NBG_TRY(alloc(e, &t->vals[0], n));
+    NBG_TRY(alloc(e, &t->vals[1], n));
+    for (int d = 0; d < 3; ++d) NBG_TRY(alloc(e, &t->lists[d], n));
+    NBG_TRY(alloc(e, &t->spare[0], n));
+    NBG_TRY(alloc(e, &t->spare[1], n));
+    NBG_TRY(alloc(e, &t->flag, n));
+    NBG_TRY(alloc(e, &t->tile_count, 2 * ntiles));
+    NBG_TRY(alloc(e, &t->hist, kDigits * nblocks));
+    NBG_TRY(alloc(e, &t->com, 3 * sz));
+    NBG_TRY(alloc(e, &t->mass, sz));
+    NBG_TRY(alloc(e, &t->bmin, 3 * sz));
+    NBG_TRY(alloc(e, &t->bmax, 3 * sz));
+    NBG_TRY(alloc(e, &t->crit2, sz));
+    NBG_TRY(alloc(e, &t->body_n, sz));
+    NBG_TRY(alloc(e, &t->node4, sz));
+    NBG_TRY(alloc(e, &t->nodem, sz));
+    NBG_TRY(alloc(e, &t->counters, 4));
+#undef NBG_TRY
+    // index 0 is unused; zero everything once so stray reads are defined
+    NBG_CUDA(e, cudaMemsetAsync(t->node4, 0, sz * sizeof(float4), e->stream));
+    NBG_CUDA(e, cudaMemsetAsync(t->nodem, 0, sz * sizeof(float), e->stream));
+    NBG_CUDA(e, cudaMemsetAsync(t->crit2, 0, sz * sizeof(double), e->stream));
+    NBG_CUDA(e, cudaMemsetAsync(t->body_n, 0, sz * sizeof(int), e->stream));
+    NBG_CUDA(e, cudaMemsetAsync(t->counters, 0, 4 * sizeof(unsigned long long), e->stream));
+    return NBG_OK;
+}
+
+nbg_status radix_sort(nbg_engine* e, TreeState* t, int n) {
+    const int nblocks = (n + kSortTile - 1) / kSortTile;
+    for (int pass = 0; pass < 8; ++pass) {
+        const int shift = 8 * pass;
+        const int src = pass & 1, dst = src ^ 1;
+        radix_hist_kernel<<<nblocks, kSortThreads, 0, e->stream>>>(t->keys[src], n, shift, t->hist);
+        NBG_LAUNCHED(e, "radix_hist_kernel");
+        radix_scan_kernel<<<1, 1024, 0, e->stream>>>(t->hist, kDigits * nblocks);
+        NBG_LAUNCHED(e, "radix_scan_kernel");
+        radix_scatter_kernel<<<nblocks, kSortThreads, 0, e->stream>>>(
+            t->keys[src], t->vals[src], t->keys[dst], t->vals[dst], n, shift, t->hist);
+        NBG_LAUNCHED(e, "radix_scatter_kernel");
+    }
+    return NBG_OK;  // 8 passes: the result is back in keys[0] / vals[0]
+}
+
+nbg_status update_levels(nbg_engine* e, TreeState* t) {
+    const double lambda2 = t->lambda * t->lambda;
+    for (int lv = t->levels - 1; lv >= 0; --lv) {
+        const int first = 1 << lv;
+        update_level_kernel<<<grid_for(first, 256, (unsigned)e->sm_count * 8u), 256, 0,
+                              e->stream>>>(first, first, lambda2, *t);
+        NBG_LAUNCHED(e, "update_level_kernel");
+    }
+    return NBG_OK;
+}
+
+}  // namespace
+
+void tree_destroy(nbg_engine* e) {
+    TreeState* t = e->tree;
+    if (t == nullptr) return;
+    void* ptrs[] = {t->keys[0], t->keys[1], t->vals[0], t->vals[1], t->lists[0], t->lists[1],
+                    t->lists[2], t->spare[0], t->spare[1], t->flag, t->tile_count, t->hist,
+                    t->com, t->mass, t->bmin, t->bmax, t->crit2, t->body_n, t->node4,
+                    t->nodem, t->feat, t->counters};
+    for (void* p : ptrs) cudaFree(p);
+    delete t;
+    e->tree = nullptr;
+}
+
+nbg_status tree_build(nbg_engine* e, const double* y) {
+    const int n = (int)e->count;
+    if (e->tree == nullptr) {
+        e->tree = new TreeState();
+        e->tree->n = (size_t)n;
+        e->tree->size = 2 * (size_t)n;
+        int k = 0;
+        while ((1 << k) < n) ++k;
+        e->tree->levels = k;
+        nbg_status s = tree_alloc(e);
+        if (s != NBG_OK) {
+            tree_destroy(e);
+            return s;
+        }
+    }
+    TreeState* t = e->tree;
+    t->lambda = e->params.distance_to_node_radius_ratio;
+    ProfScope ps(e, NBG_K_TREE_BUILD);
+    const unsigned g = grid_for(n, 256, (unsigned)e->sm_count * 8u);
+    // 1. three sorted lists
+    for (int d = 0; d < 3; ++d) {
+        init_keys_kernel<<<g, 256, 0, e->stream>>>(y + (size_t)d * n, n, t->keys[0], t->vals[0]);
+        NBG_LAUNCHED(e, "init_keys_kernel");
+        nbg_status s = radix_sort(e, t, n);
+        if (s != NBG_OK) return s;
+        NBG_CUDA(e, cudaMemcpyAsync(t->lists[d], t->vals[0], n * sizeof(int),
+                                    cudaMemcpyDeviceToDevice, e->stream));
+    }
+    // 2. median splits, level by level
+    const int ntiles = (n + kPartTile - 1) / kPartTile;
+    for (int lv = 0; lv < t->levels; ++lv) {
+        const int S = n >> lv;
+        const int d = lv % 3;
+        split_flag_kernel<<<g, 256, 0, e->stream>>>(t->lists[d], n, S, t->flag);
+        NBG_LAUNCHED(e, "split_flag_kernel");
+        const int e0 = (d + 1) % 3, e1 = (d + 2) % 3;
+        PartArgs a;
+        a.in[0] = t->lists[e0];
+        a.in[1] = t->lists[e1];
+        a.out[0] = t->spare[0];
+        a.out[1] = t->spare[1];
+        a.flag = t->flag;
+        a.tile_count = t->tile_count;
+        a.ntiles = ntiles;
+        a.n = n;
+        a.S = S;
+        if (S > kPartTile) {
+            part_count_kernel<<<dim3(ntiles, 2), 256, 0, e->stream>>>(a);
+            NBG_LAUNCHED(e, "part_count_kernel");
+        }
+        part_scatter_kernel<<<dim3(ntiles, 2), 256, 0, e->stream>>>(a);
+        NBG_LAUNCHED(e, "part_scatter_kernel");
+        int* tmp0 = t->lists[e0];
+        int* tmp1 = t->lists[e1];
+        t->lists[e0] = t->spare[0];
+        t->lists[e1] = t->spare[1];
+        t->spare[0] = tmp0;
+        t->spare[1] = tmp1;
+    }
+    // 3. leaves, then the bottom-up update
+    leaf_init_kernel<<<g, 256, 0, e->stream>>>(t->lists[0], y, e->d_mass, n, *t);
+    NBG_LAUNCHED(e, "leaf_init_kernel");
+    nbg_status s = update_levels(e, t);
+    if (s != NBG_OK) return s;
+    t->built = true;
+    return NBG_OK;
+}
+
+nbg_status tree_refit(nbg_engine* e, const double* y) {
+    TreeState* t = e->tree;
+    const int n = (int)e->count;
+    t->lambda = e->params.distance_to_node_radius_ratio;
+    ProfScope ps(e, NBG_K_TREE_BUILD);
+    leaf_refit_kernel<<<grid_for(n, 256, (unsigned)e->sm_count * 8u), 256, 0, e->stream>>>(y, n, *t);
+    NBG_LAUNCHED(e, "leaf_refit_kernel");
+    return update_levels(e, t);
+}
+
+}  // namespace nbg

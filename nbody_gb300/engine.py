@@ -421,6 +421,13 @@ class NbodyEngineGB300:
         self._check(self._lib.nbg_measure_fp32_peak(self._h, C.byref(r)), "measure_fp32_peak")
         return r.value
 
+    def bh_counters(self):
+        """(node visits, interactions) of the mixed Barnes-Hut walk since the last call."""
+        v = C.c_uint64(0)
+        i = C.c_uint64(0)
+        self._check(self._lib.nbg_bh_counters(self._h, C.byref(v), C.byref(i)), "bh_counters")
+        return v.value, i.value
+
     def tune_set(self, key: str, value: int) -> None:
         self._check(self._lib.nbg_tune_set(self._h, key.encode(), int(value)), "tune_set")
 

@@ -1,0 +1,124 @@
+"""Barnes-Hut on the GPU against the oracle restatement of simple_bh.
+
+FP64 mode reproduces the reference's cuda_bh / cuda_bh_tex vs simple_bh
+comparisons (test/engine/test_nbody_engine.cpp:1255-1336): make_universe
+N = 128 (and 1024), lambda in {3.1623, 1e8}, layouts heap / heap_stackless,
+traversals cycle / nested_tree, tree_build_rate 0 and 2 (refit on odd steps),
+two steps with y *= 1.99 between, 1e-13 absolute.  The mixed mode is judged
+against the FP64 direct sum.
+"""
+import numpy as np
+import pytest
+
+from nbody_gb300.data import NBodyData
+
+pytestmark = pytest.mark.gpu
+
+
+def _f(e, y):
+    n6 = y.size
+    my, mf = e.create_buffer(8 * n6), e.create_buffer(8 * n6)
+    e.write_buffer(my, y)
+    e.fill_buffer(mf, 1e10)
+    e.fcompute(0.0, my, mf)
+    out = np.zeros(n6)
+    e.read_buffer(out, mf)
+    e.free_buffer(my)
+    e.free_buffer(mf)
+    return out
+
+
+LAYOUT = {"heap": 1, "heap_stackless": 2}
+TRAV = {"cycle": 0, "nested_tree": 1}
+
+
+@pytest.mark.parametrize("lam", [3.1623, 1e8])
+@pytest.mark.parametrize("layout", ["heap", "heap_stackless"])
+@pytest.mark.parametrize("trav", ["cycle", "nested_tree"])
+@pytest.mark.parametrize("rate", [0, 2])
+def test_bh_fp64_vs_simple_bh(make_engine, oracle, lam, layout, trav, rate):
+    d = NBodyData.make_universe(64)  # 128 bodies
+    e = make_engine(algo="bh", precision="fp64", distance_to_node_radius_ratio=lam,
+                    tree_layout=layout, traverse_type=trav, tree_build_rate=rate)
+    assert e.init(d)
+    mut = lambda v: v + v * 0.99
+    ref = oracle.fcompute_bh(d.to_state(), d.mass, lam, layout=LAYOUT[layout],
+                             traverse=TRAV[trav], steps=2, build_rate=rate, mutate=mut)
+    y = d.to_state()
+    for step in range(2):
+        e.set_step(step)
+        f = _f(e, y)
+        assert np.max(np.abs(f - ref[step])) <= 1e-13, f"step {step}"
+        y = mut(y)
+
+
+@pytest.mark.parametrize("n", [1, 2, 4, 8, 64, 1024, 4096])
+def test_bh_fp64_sizes(make_engine, oracle, n):
+    d = NBodyData.uniform_cube(n, side=10.0, seed=n)
+    e = make_engine(algo="bh", precision="fp64", distance_to_node_radius_ratio=3.1623)
+    assert e.init(d)
+    f = _f(e, d.to_state())
+    ref = oracle.fcompute_bh(d.to_state(), d.mass, 3.1623, layout=2, traverse=1)[0]
+    assert np.max(np.abs(f - ref)) <= 1e-13 * max(1.0, np.max(np.abs(ref)))
+
+
+def test_bh_fp64_large_exact_ratio(make_engine, oracle):
+    # lambda = 1e8 opens every node: the walk is a direct sum in tree order
+    d = NBodyData.make_universe(512)  # 1024 bodies
+    e = make_engine(algo="bh", precision="fp64", distance_to_node_radius_ratio=1e8)
+    assert e.init(d)
+    f = _f(e, d.to_state())
+    ref = oracle.fcompute_simple(d.to_state(), d.mass)
+    assert np.max(np.abs(f - ref)) <= 1e-11
+
+
+def test_bh_rejects_non_power_of_two(make_engine):
+    d = NBodyData.uniform_cube(100, seed=1)
+    e = make_engine(algo="bh", precision="fp64")
+    assert not e.init(d)
+    assert e.last_status == 6  # NBG_ERR_UNSUPPORTED
+
+
+def _rel(a, a_ref):
+    return np.linalg.norm(a - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
+
+
+@pytest.mark.parametrize("lam", [2.0, 1.0 / 0.9])
+def test_bh_mixed_error_vs_direct(make_engine, oracle, lam):
+    """The warp-coherent FP32 walk is at least as accurate as the reference's
+    own per-body FP64 walk (simple_bh heap_stackless) at the same ratio, both
+    judged against the FP64 direct sum."""
+    n = 16384
+    d = NBodyData.plummer(n, seed=4)
+    y = d.to_state()
+    e = make_engine(algo="bh", precision="mixed", softening=0.0,
+                    distance_to_node_radius_ratio=lam)
+    assert e.init(d)
+    f = _f(e, y)
+    rows = np.random.default_rng(9).choice(n, size=512, replace=False)
+    a_ref = oracle.accel_rows(y, d.mass, 0.0, rows=rows)
+    a = f[3 * n:].reshape(3, n).T[rows]
+    f_bh = oracle.fcompute_bh(y, d.mass, lam, layout=2, traverse=0, nthreads=8)[0]
+    a_bh = f_bh[3 * n:].reshape(3, n).T[rows]
+    rel, rel_ref = _rel(a, a_ref), _rel(a_bh, a_ref)
+    visits, inter = e.bh_counters()
+    print(f"\nBH mixed lambda={lam:.3f}: p50 {np.median(rel):.2e} p99 {np.quantile(rel, 0.99):.2e}"
+          f" (reference walk p50 {np.median(rel_ref):.2e} p99 {np.quantile(rel_ref, 0.99):.2e});"
+          f" interactions/body {inter / n:.0f}, visits/warp {visits / (n / 32):.0f}")
+    assert np.array_equal(f[:3 * n], y[3 * n:])
+    assert np.quantile(rel, 0.99) <= np.quantile(rel_ref, 0.99)
+    assert np.median(rel) <= np.median(rel_ref)
+
+
+def test_bh_mixed_refit_path(make_engine):
+    n = 4096
+    d = NBodyData.plummer(n, seed=5)
+    e = make_engine(algo="bh", precision="mixed", softening=1e-3,
+                    distance_to_node_radius_ratio=2.0, tree_build_rate=2)
+    assert e.init(d)
+    y = d.to_state()
+    e.set_step(0)
+    f0 = _f(e, y)
+    e.set_step(1)  # refit: same bodies per leaf, same positions -> same forces
+    f1 = _f(e, y)
+    assert np.max(np.abs(f0 - f1)) == 0.0
