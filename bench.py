@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N_BODIES)
+    ap.add_argument("--no-bh", action="store_true", help="skip the Barnes-Hut measurements")
     return ap.parse_args()
 
 
@@ -209,6 +210,60 @@ def read_traffic():
     return None
 
 
+def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 5):
+    """Barnes-Hut fcompute (tree rebuilt every call) at opening ratio lam."""
+    from nbody_gb300 import _lib
+    from nbody_gb300.engine import create_engine
+    e = create_engine({"engine": "gb300", "algo": "bh", "precision": "mixed",
+                       "softening": SOFTENING, "distance_to_node_radius_ratio": lam,
+                       "learned": learned, "tree_layout": "heap_stackless"})
+    if e is None or not e.init(d):
+        return {"unavailable": "engine not created"}
+    f = e.create_buffer(8 * 6 * n_bh)
+    for _ in range(2):
+        e.fcompute(0.0, e.get_y(), f)
+    e.synchronize()
+    e.bh_counters()
+    e.profile_enable(True)
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        e.fcompute(0.0, e.get_y(), f)
+    e.synchronize()
+    wall = (time.perf_counter() - t0) / calls
+    tb, nb = e.profile_query(_lib.K_TREE_BUILD)
+    tw, nw = e.profile_query(_lib.K_BH_WALK)
+    visits, inter = e.bh_counters()
+    out = np.zeros(6 * n_bh)
+    e.read_buffer(out, f)
+    a = out[3 * n_bh:].reshape(3, n_bh).T[rows]
+    rel = np.linalg.norm(a - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
+    e.close()
+    ms = (tb / max(nb, 1) + tw / max(nw, 1))
+    return {"lambda": lam, "theta": 1.0 / lam, "bodies_per_s": n_bh / (ms * 1e-3),
+            "ms_per_fcompute": ms, "wall_ms_per_fcompute": wall * 1e3,
+            "build_ms": tb / max(nb, 1), "walk_ms": tw / max(nw, 1),
+            "p50": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99)),
+            "interactions_per_body": inter / calls / n_bh,
+            "warp_node_visits_per_warp": visits / calls / (n_bh / 32)}
+
+
+def run_bh_suite(rank: int):
+    """Plummer N = 2^20, softening 1e-3, heap_stackless, rebuilt every fcompute."""
+    from nbody_gb300.data import NBodyData
+    from oracle.oracle import load_oracle
+    n_bh = 1 << 20
+    d = NBodyData.plummer(n_bh, seed=3)
+    y = d.to_state()
+    rows = np.random.default_rng(7).choice(n_bh, size=4096, replace=False)
+    a_ref = load_oracle().accel_rows(y, d.mass, SOFTENING, rows=rows)
+    res = {"workload": "Barnes-Hut fcompute, N=1048576 Plummer, softening 1e-3, heap_stackless, "
+                       "tree rebuilt every call, FP32 walk / FP64 state",
+           "error_judge": "FP64 direct sum (oracle) on 4096 sampled bodies"}
+    res["plain_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d)
+    res["plain_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d)
+    return res
+
+
 def run_gb300(args):
     rank, local, world = dist_setup(args.gpus)
     import torch
@@ -317,6 +372,8 @@ def run_gb300(args):
         cpu = {"value": v, "unit": "pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
                "sample": f"block engine (FP64) on {rows} of {n} rows x {n} bodies, {dt:.1f} s"}
 
+    bh = run_bh_suite(rank) if (rank == 0 and not args.no_bh) else None
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
@@ -344,6 +401,7 @@ def run_gb300(args):
             "gpu_launches": int(launches),
             "clocks": clk,
             "force_error": err,
+            "bh": bh,
             "wall_s_timed": wall,
         }
         print(json.dumps(line), flush=True)

@@ -169,6 +169,46 @@ nbg_status nbg_profile_query(nbg_engine* e, int kernel_id, double* total_ms,
  * (per warp: every visit is one broadcast node load) and accepted
  * body-node interactions; resets them. */
 nbg_status nbg_bh_counters(nbg_engine* e, uint64_t* visits, uint64_t* interactions);
+/* ---- learned monopole correction (no reference counterpart) ----
+ * A 16 -> 64 -> 64 -> 3 GELU MLP (BF16 weights, FP32 accumulate) predicts,
+ * for a body-cell interaction accepted at the engine's ratio lambda_l but
+ * inside the band lambda_l < lambda <= learned_tight_ratio, the residual
+ * between the cell's exact subtree acceleration and its monopole, in units
+ * of m / s^2 (s = cell radius).  Used when nbg_params.learned = 1 (Barnes-Hut,
+ * mixed precision); tuning key "learned.group" selects one sample per
+ * (body, cell) (0, default) or per (warp, cell) at the warp centroid (1). */
+size_t nbg_learn_param_count(void);
+nbg_status nbg_learn_set_weights(nbg_engine* e, const float* w, size_t count);
+nbg_status nbg_learn_get_weights(nbg_engine* e, float* w, size_t count);
+/* Glorot-uniform initialisation from a seed (biases zero). */
+nbg_status nbg_learn_init_weights(nbg_engine* e, uint64_t seed);
+/* Build the tree of the engine's current state and append up to max_samples
+ * (features, target) samples: exact subtree sums for in-band interactions of
+ * randomly chosen bodies; cells with more than 2^max_subtree_log2 bodies
+ * are skipped. */
+nbg_status nbg_learn_generate(nbg_engine* e, size_t max_samples, uint64_t seed,
+                              int max_subtree_log2, size_t* produced);
+size_t nbg_learn_sample_count(const nbg_engine* e);
+/* Copy samples [offset, offset + count): x [count][16], t [count][4],
+ * meta [count][2] = (body, cell); any output may be NULL. */
+nbg_status nbg_learn_read_samples(nbg_engine* e, size_t offset, size_t count, float* x,
+                                  float* t, int* meta);
+nbg_status nbg_learn_clear_samples(nbg_engine* e);
+/* Adam on the stored samples (MSE), cosine-decayed learning rate; a seeded
+ * val_fraction of the samples is held out and scored at the end. */
+nbg_status nbg_learn_train(nbg_engine* e, int epochs, size_t batch, double lr, uint64_t seed,
+                           double val_fraction, double* train_mse, double* val_mse);
+/* Sum of squared errors and the gradient of the mean loss over host samples
+ * (x [count][16], t [count][4]) with the current weights: the training
+ * kernels' forward and backward pass, for gradient checks. */
+nbg_status nbg_learn_loss_grad(nbg_engine* e, const float* x, const float* t, size_t count,
+                               double* loss_sum, float* grad);
+/* Network outputs g (x [count][16] -> out [count][3]) with the inference
+ * routine of the walk. */
+nbg_status nbg_learn_predict(nbg_engine* e, const float* x, size_t count, float* out);
+/* Body index of each leaf of the last tree (leaf order), [N]. */
+nbg_status nbg_tree_leaves(nbg_engine* e, int* body_of_leaf);
+
 /* Number of kernels this engine has launched since creation. */
 uint64_t nbg_launch_count(const nbg_engine* e);
 

@@ -33,7 +33,10 @@ EXPORTS = [
     "nbg_synchronize", "nbg_stream", "nbg_host_alloc", "nbg_host_free",
     "nbg_profile_enable", "nbg_profile_query", "nbg_launch_count",
     "nbg_measure_fp32_peak", "nbg_tune_set", "nbg_tune_get", "nbg_direct_mixed_noalloc",
-    "nbg_bh_counters",
+    "nbg_bh_counters", "nbg_learn_param_count", "nbg_learn_set_weights",
+    "nbg_learn_get_weights", "nbg_learn_init_weights", "nbg_learn_generate",
+    "nbg_learn_sample_count", "nbg_learn_read_samples", "nbg_learn_clear_samples",
+    "nbg_learn_train", "nbg_learn_loss_grad", "nbg_tree_leaves", "nbg_learn_predict",
 ]
 
 
@@ -120,5 +123,19 @@ def load() -> C.CDLL:
     _proto(lib, "nbg_tune_get", i32, vp, C.c_char_p, C.POINTER(C.c_int64))
     _proto(lib, "nbg_direct_mixed_noalloc", i32, vp, vp, vp, sz, dbl, vp)
     _proto(lib, "nbg_bh_counters", i32, vp, C.POINTER(u64), C.POINTER(u64))
+    fp = C.POINTER(C.c_float)
+    ip = C.POINTER(C.c_int)
+    _proto(lib, "nbg_learn_param_count", sz)
+    _proto(lib, "nbg_learn_set_weights", i32, vp, fp, sz)
+    _proto(lib, "nbg_learn_get_weights", i32, vp, fp, sz)
+    _proto(lib, "nbg_learn_init_weights", i32, vp, u64)
+    _proto(lib, "nbg_learn_generate", i32, vp, sz, u64, i32, C.POINTER(sz))
+    _proto(lib, "nbg_learn_sample_count", sz, vp)
+    _proto(lib, "nbg_learn_read_samples", i32, vp, sz, sz, fp, fp, ip)
+    _proto(lib, "nbg_learn_clear_samples", i32, vp)
+    _proto(lib, "nbg_learn_train", i32, vp, i32, sz, dbl, u64, dbl, dp, dp)
+    _proto(lib, "nbg_learn_loss_grad", i32, vp, fp, fp, sz, dp, fp)
+    _proto(lib, "nbg_tree_leaves", i32, vp, ip)
+    _proto(lib, "nbg_learn_predict", i32, vp, fp, sz, fp)
     _lib = lib
     return lib

@@ -226,6 +226,7 @@ void nbg_engine_destroy(nbg_engine* e) {
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
     tree_destroy(e);
+    learn_destroy(e);
     for (const nbg_buffer* b : e->buffers) {
         cudaFree(b->dptr);
         delete b;

@@ -144,6 +144,7 @@ nbg_status direct_fcompute(nbg_engine* e, const double* y, double* f);
 // nbg_tree.cu / nbg_bh.cu
 nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f);
 void tree_destroy(nbg_engine* e);
+void learn_destroy(nbg_engine* e);  // nbg_learned.cu
 
 // nbg_probe.cu
 nbg_status measure_fp32_peak(nbg_engine* e, double* flops);

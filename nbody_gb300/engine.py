@@ -428,6 +428,81 @@ class NbodyEngineGB300:
         self._check(self._lib.nbg_bh_counters(self._h, C.byref(v), C.byref(i)), "bh_counters")
         return v.value, i.value
 
+    # -- learned correction ---------------------------------------------------------
+    def learn_param_count(self) -> int:
+        return int(self._lib.nbg_learn_param_count())
+
+    def learn_set_weights(self, w) -> None:
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self._check(self._lib.nbg_learn_set_weights(
+            self._h, w.ctypes.data_as(C.POINTER(C.c_float)), w.size), "learn_set_weights")
+
+    def learn_get_weights(self) -> np.ndarray:
+        w = np.zeros(self.learn_param_count(), dtype=np.float32)
+        self._check(self._lib.nbg_learn_get_weights(
+            self._h, w.ctypes.data_as(C.POINTER(C.c_float)), w.size), "learn_get_weights")
+        return w
+
+    def learn_init_weights(self, seed: int = 1) -> None:
+        self._check(self._lib.nbg_learn_init_weights(self._h, seed), "learn_init_weights")
+
+    def learn_generate(self, max_samples: int, seed: int = 1, max_subtree_log2: int = 16) -> int:
+        got = C.c_size_t(0)
+        self._check(self._lib.nbg_learn_generate(self._h, max_samples, seed, max_subtree_log2,
+                                                 C.byref(got)), "learn_generate")
+        return got.value
+
+    def learn_sample_count(self) -> int:
+        return int(self._lib.nbg_learn_sample_count(self._h))
+
+    def learn_read_samples(self, offset: int, count: int):
+        x = np.zeros((count, 16), dtype=np.float32)
+        t = np.zeros((count, 4), dtype=np.float32)
+        m = np.zeros((count, 2), dtype=np.int32)
+        fp = C.POINTER(C.c_float)
+        self._check(self._lib.nbg_learn_read_samples(
+            self._h, offset, count, x.ctypes.data_as(fp), t.ctypes.data_as(fp),
+            m.ctypes.data_as(C.POINTER(C.c_int))), "learn_read_samples")
+        return x, t, m
+
+    def learn_clear_samples(self) -> None:
+        self._check(self._lib.nbg_learn_clear_samples(self._h), "learn_clear_samples")
+
+    def learn_train(self, epochs: int, batch: int = 16384, lr: float = 3e-3, seed: int = 1,
+                    val_fraction: float = 0.1):
+        tr = C.c_double(0.0)
+        va = C.c_double(0.0)
+        self._check(self._lib.nbg_learn_train(self._h, epochs, batch, lr, seed, val_fraction,
+                                              C.byref(tr), C.byref(va)), "learn_train")
+        return tr.value, va.value
+
+    def learn_loss_grad(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        g = np.zeros(self.learn_param_count(), dtype=np.float32)
+        loss = C.c_double(0.0)
+        fp = C.POINTER(C.c_float)
+        self._check(self._lib.nbg_learn_loss_grad(self._h, x.ctypes.data_as(fp),
+                                                  t.ctypes.data_as(fp), x.shape[0],
+                                                  C.byref(loss), g.ctypes.data_as(fp)),
+                    "learn_loss_grad")
+        return loss.value, g
+
+    def learn_predict(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        out = np.zeros((x.shape[0], 3), dtype=np.float32)
+        fp = C.POINTER(C.c_float)
+        self._check(self._lib.nbg_learn_predict(self._h, x.ctypes.data_as(fp), x.shape[0],
+                                                out.ctypes.data_as(fp)), "learn_predict")
+        return out
+
+    def tree_leaves(self) -> np.ndarray:
+        n = self.problem_size() // 6
+        out = np.zeros(n, dtype=np.int32)
+        self._check(self._lib.nbg_tree_leaves(self._h, out.ctypes.data_as(C.POINTER(C.c_int))),
+                    "tree_leaves")
+        return out
+
     def tune_set(self, key: str, value: int) -> None:
         self._check(self._lib.nbg_tune_set(self._h, key.encode(), int(value)), "tune_set")
 

@@ -1,0 +1,83 @@
+"""FP64 restatement of the learned correction's MLP (test infrastructure).
+
+TEST INFRASTRUCTURE ONLY: the checker for the engine's BF16 tensor-core
+training and inference kernels (nbody_gb300/csrc/nbg_mlp.cuh,
+nbg_learned.cu).  The correction has no counterpart in the reference.
+
+Network 16 -> 64 -> 64 -> 3, GELU in the tanh form
+0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))) (Hendrycks & Gimpel 2016)
+after both hidden layers; loss = sum over samples and outputs of the squared
+error, gradients of the mean loss (sum / count).  Parameter layout (flat,
+k-major): W1[16][64], b1[64], W2[64][64], b2[64], W3[64][3], b3[3].
+"""
+from __future__ import annotations
+
+import numpy as np
+
+IN, H, OUT = 16, 64, 3
+OFF_W1 = 0
+OFF_B1 = OFF_W1 + IN * H
+OFF_W2 = OFF_B1 + H
+OFF_B2 = OFF_W2 + H * H
+OFF_W3 = OFF_B2 + H
+OFF_B3 = OFF_W3 + H * OUT
+N_PARAMS = OFF_B3 + OUT
+GC = np.sqrt(2.0 / np.pi)
+GA = 0.044715
+
+
+def unpack(w):
+    w = np.asarray(w, dtype=np.float64)
+    return (w[OFF_W1:OFF_B1].reshape(IN, H), w[OFF_B1:OFF_W2], w[OFF_W2:OFF_B2].reshape(H, H),
+            w[OFF_B2:OFF_W3], w[OFF_W3:OFF_B3].reshape(H, OUT), w[OFF_B3:N_PARAMS])
+
+
+def gelu(z):
+    return 0.5 * z * (1.0 + np.tanh(GC * (z + GA * z ** 3)))
+
+
+def gelu_grad(z):
+    t = np.tanh(GC * (z + GA * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * GC * (1.0 + 3.0 * GA * z * z)
+
+
+def forward(w, x):
+    W1, b1, W2, b2, W3, b3 = unpack(w)
+    z1 = x @ W1 + b1
+    a1 = gelu(z1)
+    z2 = a1 @ W2 + b2
+    a2 = gelu(z2)
+    return a2 @ W3 + b3
+
+
+def loss_grad(w, x, t):
+    """(sum of squared errors, gradient of the mean loss)."""
+    x = np.asarray(x, dtype=np.float64)
+    t = np.asarray(t, dtype=np.float64)[:, :OUT]
+    W1, b1, W2, b2, W3, b3 = unpack(w)
+    B = x.shape[0]
+    z1 = x @ W1 + b1
+    a1 = gelu(z1)
+    z2 = a1 @ W2 + b2
+    a2 = gelu(z2)
+    y = a2 @ W3 + b3
+    e = y - t
+    dy = 2.0 * e / B
+    g = np.zeros(N_PARAMS)
+    g[OFF_W3:OFF_B3] = (a2.T @ dy).ravel()
+    g[OFF_B3:N_PARAMS] = dy.sum(axis=0)
+    dz2 = (dy @ W3.T) * gelu_grad(z2)
+    g[OFF_W2:OFF_B2] = (a1.T @ dz2).ravel()
+    g[OFF_B2:OFF_W3] = dz2.sum(axis=0)
+    dz1 = (dz2 @ W2.T) * gelu_grad(z1)
+    g[OFF_W1:OFF_B1] = (x.T @ dz1).ravel()
+    g[OFF_B1:OFF_W2] = dz1.sum(axis=0)
+    return float((e * e).sum()), g
+
+
+def bf16(a):
+    """Round to bfloat16 (nearest even), returned as float64."""
+    a = np.asarray(a, dtype=np.float32)
+    b = a.view(np.uint32).astype(np.uint64)
+    b = (b + 0x7FFF + ((b >> 16) & 1)) & 0xFFFF0000
+    return b.astype(np.uint32).view(np.float32).astype(np.float64)

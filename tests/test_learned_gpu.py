@@ -1,0 +1,196 @@
+"""The learned monopole correction: sample generation, BF16 tensor-core
+training kernels (gradients against an FP64 restatement), the inference
+routine against the FP64 forward pass, and the measured change of the force
+error that the trained network brings over plain Barnes-Hut at theta = 0.9."""
+import numpy as np
+import pytest
+
+from nbody_gb300.data import NBodyData
+from oracle import mlp_oracle as M
+
+pytestmark = pytest.mark.gpu
+
+EPS = 1e-3
+
+
+def _bh_engine(make_engine, lam, learned=False, tight=2.0):
+    return make_engine(algo="bh", precision="mixed", softening=EPS,
+                       distance_to_node_radius_ratio=lam, learned=learned,
+                       learned_tight_ratio=tight)
+
+
+def test_param_count(gpulib):
+    assert gpulib.nbg_learn_param_count() == M.N_PARAMS == 5443
+
+
+def test_gradient_matches_fp64_restatement(make_engine):
+    """Forward/backward of the training kernels vs FP64 numpy on the same
+    (BF16-representable) weights and inputs."""
+    e = _bh_engine(make_engine, 1.0 / 0.9)
+    d = NBodyData.plummer(1024, seed=2)
+    assert e.init(d)
+    rng = np.random.default_rng(3)
+    w = M.bf16(rng.normal(0, 0.3, size=M.N_PARAMS)).astype(np.float32)
+    e.learn_set_weights(w)
+    x = M.bf16(rng.normal(0, 1.0, size=(96, 16))).astype(np.float32)
+    t = np.zeros((96, 4), dtype=np.float32)
+    t[:, :3] = rng.normal(0, 0.5, size=(96, 3))
+    loss_gpu, g_gpu = e.learn_loss_grad(x, t)
+    loss_ref, g_ref = M.loss_grad(w, x, t)
+    assert abs(loss_gpu - loss_ref) <= 2e-2 * loss_ref
+    # BF16 activations between layers: compare the gradient as a vector
+    err = np.linalg.norm(g_gpu - g_ref) / np.linalg.norm(g_ref)
+    cos = g_gpu @ g_ref / (np.linalg.norm(g_gpu) * np.linalg.norm(g_ref))
+    print(f"\ngrad check: rel err {err:.3e}, cosine {cos:.6f}, loss {loss_gpu:.4e} vs {loss_ref:.4e}")
+    assert err < 3e-2 and cos > 0.999
+    # every parameter block carries gradient
+    for a, b in ((M.OFF_W1, M.OFF_B1), (M.OFF_B1, M.OFF_W2), (M.OFF_W2, M.OFF_B2),
+                 (M.OFF_B2, M.OFF_W3), (M.OFF_W3, M.OFF_B3), (M.OFF_B3, M.N_PARAMS)):
+        blk = np.linalg.norm(g_gpu[a:b] - g_ref[a:b]) / np.linalg.norm(g_ref[a:b])
+        assert blk < 5e-2, (a, b, blk)
+
+
+def _subtree(leaves, n, node):
+    k = n.bit_length() - 1
+    lv = node.bit_length() - 1
+    span = 1 << (k - lv)
+    first = (node << (k - lv)) - n
+    return leaves[first:first + span]
+
+
+def test_samples_match_cpu_recomputation(make_engine):
+    """Targets and features of generated samples recomputed on the CPU from
+    the tree's leaf order: exact subtree sum minus monopole, scaled s^2/m."""
+    n = 4096
+    lam = 1.0 / 0.9
+    d = NBodyData.plummer(n, seed=6)
+    e = _bh_engine(make_engine, lam)
+    assert e.init(d)
+    got = e.learn_generate(20000, seed=2)
+    assert got > 1000
+    leaves = e.tree_leaves()
+    assert sorted(leaves.tolist()) == list(range(n))
+    x, t, meta = e.learn_read_samples(0, got)
+    pos, mass = d.vertices, d.mass
+    rng = np.random.default_rng(0)
+    for k in rng.choice(got, size=60, replace=False):
+        b, node = int(meta[k, 0]), int(meta[k, 1])
+        bodies = _subtree(leaves, n, node)
+        assert b not in set(bodies.tolist())
+        m = mass[bodies].sum()
+        com = (pos[bodies] * mass[bodies, None]).sum(axis=0) / m
+        bmin, bmax = pos[bodies].min(axis=0), pos[bodies].max(axis=0)
+        s = np.linalg.norm(bmax - bmin) * 0.5 + np.linalg.norm((bmax + bmin) / 2 - com)
+        dr = pos[bodies] - pos[b]
+        r2 = (dr * dr).sum(axis=1) + EPS * EPS
+        exact = (dr * (mass[bodies] / (r2 * np.sqrt(r2)))[:, None]).sum(axis=0)
+        dc = com - pos[b]
+        rc2 = dc @ dc + EPS * EPS
+        mono = dc * m / (rc2 * np.sqrt(rc2))
+        target = (exact - mono) * s * s / m
+        scale = max(np.abs(target).max(), 1e-3)
+        assert np.allclose(t[k, :3], target, atol=2e-4 * scale + 1e-6), (k, t[k, :3], target)
+        u = (pos[b] - com) / s
+        assert np.allclose(x[k, :3], u, rtol=1e-4, atol=1e-4)
+        q = np.einsum("k,ka,kb->ab", mass[bodies], pos[bodies] - com, pos[bodies] - com) / (m * s * s)
+        qv = [q[0, 0], q[1, 1], q[2, 2], q[0, 1], q[0, 2], q[1, 2]]
+        assert np.allclose(x[k, 3:9], qv, rtol=1e-3, atol=1e-5)
+        assert np.allclose(x[k, 9:12], (bmax - bmin) / (2 * s), rtol=1e-4, atol=1e-5)
+        assert np.isclose(x[k, 12], 1 / np.linalg.norm(u), rtol=1e-4)
+        assert np.allclose(x[k, 13:16], (com - (bmax + bmin) / 2) / s, rtol=1e-3, atol=1e-5)
+        # inside the band: accepted at lam, opened at the tight ratio 2
+        dist = np.linalg.norm(dc)
+        assert lam * s < dist * (1 + 1e-4) and dist <= 2.0 * s * (1 + 1e-4)
+
+
+def _trained_weights(make_engine, epochs=20):
+    e = _bh_engine(make_engine, 1.0 / 0.9)
+    total = 0
+    for i, (n, kind) in enumerate(((1 << 14, "plummer"), (1 << 15, "cube"), (1 << 16, "plummer"))):
+        d = NBodyData.plummer(n, seed=10 + i) if kind == "plummer" else \
+            NBodyData.uniform_cube(n, side=2.0, seed=10 + i)
+        assert e.init(d)
+        total += e.learn_generate(400000, seed=20 + i)
+    x, t, _ = e.learn_read_samples(0, total)
+    var0 = float((t[:, :3].astype(np.float64) ** 2).mean())
+    tr, va = e.learn_train(epochs, batch=8192, lr=3e-3, seed=5)
+    print(f"\nsamples {total}, target mean square {var0:.3e}, train MSE {tr:.3e}, val MSE {va:.3e}")
+    return e.learn_get_weights(), var0, tr, va
+
+
+@pytest.fixture(scope="module")
+def trained(request):
+    from nbody_gb300.engine import create_engine
+    made = []
+
+    def mk(**param):
+        param.setdefault("engine", "gb300")
+        eng = create_engine(param)
+        made.append(eng)
+        return eng
+    res = _trained_weights(mk)
+    for eng in made:
+        eng.close()
+    return res
+
+
+def test_training_fits_the_residual(trained):
+    w, var0, tr, va = trained
+    assert np.all(np.isfinite(w))
+    # An FP32 fit of the same network plateaus near 70 % explained mean
+    # square on these features (the residual at 1.1 < d/s <= 2 is dominated
+    # by multipoles above the quadrupole); require at least 55 %.
+    assert va < 0.45 * var0
+
+
+def test_inference_path_matches_fp64_forward(make_engine, trained):
+    """The walk's tensor-core inference routine against the FP64 forward pass
+    on the same weights."""
+    w = trained[0]
+    e = _bh_engine(make_engine, 1.0 / 0.9, learned=True)
+    d = NBodyData.plummer(1024, seed=1)
+    assert e.init(d)
+    e.learn_set_weights(w)
+    rng = np.random.default_rng(8)
+    x = rng.normal(0, 0.7, size=(1000, 16)).astype(np.float32)
+    x[:, 12] = np.abs(x[:, 12])
+    got = e.learn_predict(x)
+    ref = M.forward(M.bf16(w), M.bf16(x))
+    assert np.linalg.norm(got - ref) <= 3e-2 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("group", [0, 1])
+def test_learned_walk_vs_plain(make_engine, oracle, trained, group):
+    """What the trained network changes in the force at theta = 0.9, judged by
+    the FP64 direct sum on a snapshot the network never saw.  Recorded, with
+    theta = 0.5 beside it; the assertions cover what must hold: finite forces
+    and velocity rows copied exactly, and the learned walk visiting the same
+    nodes as the plain walk at the same ratio."""
+    w = trained[0]
+    n = 1 << 15
+    d = NBodyData.plummer(n, seed=77)
+    y = d.to_state()
+    rows = np.random.default_rng(4).choice(n, size=512, replace=False)
+    a_ref = oracle.accel_rows(y, d.mass, EPS, rows=rows)
+
+    def run(lam, learned):
+        e = _bh_engine(make_engine, lam, learned=learned)
+        assert e.init(d)
+        if learned:
+            e.learn_set_weights(w)
+            e.tune_set("learned.group", group)
+        f = e.create_buffer(8 * 6 * n)
+        e.fcompute(0.0, e.get_y(), f)
+        out = np.zeros(6 * n)
+        e.read_buffer(out, f)
+        assert np.all(np.isfinite(out))
+        assert np.array_equal(out[:3 * n], y[3 * n:])
+        a = out[3 * n:].reshape(3, n).T[rows]
+        return np.linalg.norm(a - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1), e.bh_counters()
+
+    (plain09, c0), (learn09, c1), (plain05, _) = run(1 / 0.9, False), run(1 / 0.9, True), run(2.0, False)
+    q = lambda r: f"p50 {np.median(r):.3e} p99 {np.quantile(r, 0.99):.3e}"
+    print(f"\ngroup={group}: plain theta0.9 {q(plain09)} | learned theta0.9 {q(learn09)} | "
+          f"plain theta0.5 {q(plain05)}")
+    assert c0 == c1  # same walk: the correction adds work, never changes the visit sequence
+    assert np.median(learn09) < 10 * np.median(plain09)
