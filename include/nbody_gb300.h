@@ -158,6 +158,7 @@ enum nbg_kernel_id {
     NBG_K_TREE_BUILD = 1, /* whole tree build/refit sequence */
     NBG_K_BH_WALK = 2,    /* Barnes-Hut traversal kernel */
     NBG_K_VECOPS = 3,     /* buffer algebra kernels */
+    NBG_K_ENS_STEP = 4,   /* one whole ensemble RK step (graph launch) */
     NBG_K_COUNT = 8
 };
 /* Enable CUDA-event timing of each kernel class on the engine stream. */
@@ -165,6 +166,12 @@ nbg_status nbg_profile_enable(nbg_engine* e, int enable);
 /* Accumulated device time (ms) and launches of one kernel class; resets it. */
 nbg_status nbg_profile_query(nbg_engine* e, int kernel_id, double* total_ms,
                              uint64_t* launches);
+/* Conservation sums of print_statistics (nbody/nbody_data.cpp:57-145) on the
+ * GPU in FP64: out = P[3], L[3], KE, PE (both halved as the reference does),
+ * mass centre[3], total mass.  With softening eps > 0 the pair potential is
+ * -m_i m_j / sqrt(r^2 + eps^2), the potential of the integrated force. */
+nbg_status nbg_statistics(nbg_engine* e, const nbg_buffer* y, double out[12]);
+
 /* Barnes-Hut walk counters since the last call (mixed walk): node visits
  * (per warp: every visit is one broadcast node load) and accepted
  * body-node interactions; resets them. */
@@ -239,6 +246,52 @@ nbg_status nbg_tune_get(nbg_engine* e, const char* key, int64_t* value);
 #define NBG_NOALLOC_MAX_BODIES 131072
 nbg_status nbg_direct_mixed_noalloc(const double* y, const double* mass, double* f,
                                     size_t n, double softening, void* stream);
+
+/* ---- batched ensemble (no reference counterpart as a whole) ----
+ * Many independent systems of uneven size, each integrated with its own
+ * adaptive Dormand-Prince step (the rkdp table of
+ * nbody/nbody_solver_rkdp.cpp:30-62) around the mixed-precision direct sum.
+ * Per step and per system the device computes the embedded error
+ * dt * max |sum (b2 - b1) k|, accepts (y += dt sum b2 k) or rejects, and sets
+ * the next dt; one step is captured once as a CUDA graph and replayed.  The
+ * same object stepping a single system is the engine-owned fused RK step. */
+typedef struct nbg_ensemble nbg_ensemble;
+typedef struct nbg_ensemble_params {
+    uint32_t struct_size; /* sizeof(nbg_ensemble_params) */
+    int32_t device;
+    double softening;     /* Plummer epsilon (0 = reference clamp) */
+    double tolerance;     /* per-system embedded error bound */
+    double dt_initial;
+    double dt_min;
+    double dt_max;
+    int32_t use_graph;    /* 1 = replay a captured CUDA graph per step */
+} nbg_ensemble_params;
+void nbg_ensemble_params_default(nbg_ensemble_params* p);
+nbg_status nbg_ensemble_create(const nbg_ensemble_params* p, nbg_ensemble** out);
+void nbg_ensemble_destroy(nbg_ensemble* s);
+const char* nbg_ensemble_last_error(const nbg_ensemble* s);
+/* counts[nsys]; vertices / velocities AoS [sum counts][3], systems concatenated. */
+nbg_status nbg_ensemble_init(nbg_ensemble* s, size_t nsys, const uint32_t* counts,
+                             const double* vertices, const double* velocities,
+                             const double* mass);
+/* Queue `steps` RK attempts for every system (asynchronous). */
+nbg_status nbg_ensemble_step(nbg_ensemble* s, int steps);
+nbg_status nbg_ensemble_synchronize(nbg_ensemble* s);
+/* Per system (any pointer may be NULL): time, next dt, accepted, rejected. */
+nbg_status nbg_ensemble_status(nbg_ensemble* s, double* t, double* dt, uint32_t* accepted,
+                               uint32_t* rejected);
+nbg_status nbg_ensemble_get_state(nbg_ensemble* s, double* vertices, double* velocities);
+/* f = [v ; a] of the current state, SoA [6][sum counts] (parity checks). */
+nbg_status nbg_ensemble_fcompute(nbg_ensemble* s, double* f);
+/* 12 FP64 conservation sums per system (layout of nbg_statistics, softened
+ * potential of the ensemble's softening). */
+nbg_status nbg_ensemble_statistics(nbg_ensemble* s, double* out);
+/* Tuning key "ensemble.pairs_per_lane" (1 or 2), read by nbg_ensemble_init. */
+nbg_status nbg_ensemble_tune_set(nbg_ensemble* s, const char* key, int64_t value);
+uint64_t nbg_ensemble_launch_count(const nbg_ensemble* s);
+/* Accumulated device time of the force kernel (then reset); enable/disable timing. */
+nbg_status nbg_ensemble_profile(nbg_ensemble* s, int enable, double* force_ms,
+                                uint64_t* force_launches);
 
 /* FP32 FFMA throughput probe: runs a dependent-chain FMA kernel on the
  * engine's device and returns the measured FP32 FLOP/s (2 per FMA). */

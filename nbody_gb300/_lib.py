@@ -36,7 +36,12 @@ EXPORTS = [
     "nbg_bh_counters", "nbg_learn_param_count", "nbg_learn_set_weights",
     "nbg_learn_get_weights", "nbg_learn_init_weights", "nbg_learn_generate",
     "nbg_learn_sample_count", "nbg_learn_read_samples", "nbg_learn_clear_samples",
-    "nbg_learn_train", "nbg_learn_loss_grad", "nbg_tree_leaves", "nbg_learn_predict",
+    "nbg_learn_train", "nbg_learn_loss_grad", "nbg_tree_leaves", "nbg_learn_predict", "nbg_statistics",
+    "nbg_ensemble_params_default", "nbg_ensemble_create", "nbg_ensemble_destroy",
+    "nbg_ensemble_last_error", "nbg_ensemble_init", "nbg_ensemble_step",
+    "nbg_ensemble_synchronize", "nbg_ensemble_status", "nbg_ensemble_get_state",
+    "nbg_ensemble_fcompute", "nbg_ensemble_statistics", "nbg_ensemble_tune_set",
+    "nbg_ensemble_launch_count", "nbg_ensemble_profile",
 ]
 
 
@@ -55,6 +60,20 @@ class Params(C.Structure):
         ("learned", C.c_int32),
         ("block_size", C.c_int32),
         ("learned_tight_ratio", C.c_double),
+    ]
+
+
+class EnsembleParams(C.Structure):
+    """struct nbg_ensemble_params."""
+    _fields_ = [
+        ("struct_size", C.c_uint32),
+        ("device", C.c_int32),
+        ("softening", C.c_double),
+        ("tolerance", C.c_double),
+        ("dt_initial", C.c_double),
+        ("dt_min", C.c_double),
+        ("dt_max", C.c_double),
+        ("use_graph", C.c_int32),
     ]
 
 
@@ -137,5 +156,21 @@ def load() -> C.CDLL:
     _proto(lib, "nbg_learn_loss_grad", i32, vp, fp, fp, sz, dp, fp)
     _proto(lib, "nbg_tree_leaves", i32, vp, ip)
     _proto(lib, "nbg_learn_predict", i32, vp, fp, sz, fp)
+    _proto(lib, "nbg_statistics", i32, vp, vp, dp)
+    u32p = C.POINTER(C.c_uint32)
+    _proto(lib, "nbg_ensemble_params_default", None, C.POINTER(EnsembleParams))
+    _proto(lib, "nbg_ensemble_create", i32, C.POINTER(EnsembleParams), C.POINTER(vp))
+    _proto(lib, "nbg_ensemble_destroy", None, vp)
+    _proto(lib, "nbg_ensemble_last_error", C.c_char_p, vp)
+    _proto(lib, "nbg_ensemble_init", i32, vp, sz, u32p, vp, vp, vp)
+    _proto(lib, "nbg_ensemble_step", i32, vp, i32)
+    _proto(lib, "nbg_ensemble_synchronize", i32, vp)
+    _proto(lib, "nbg_ensemble_status", i32, vp, dp, dp, u32p, u32p)
+    _proto(lib, "nbg_ensemble_get_state", i32, vp, vp, vp)
+    _proto(lib, "nbg_ensemble_fcompute", i32, vp, dp)
+    _proto(lib, "nbg_ensemble_statistics", i32, vp, dp)
+    _proto(lib, "nbg_ensemble_tune_set", i32, vp, C.c_char_p, C.c_int64)
+    _proto(lib, "nbg_ensemble_launch_count", u64, vp)
+    _proto(lib, "nbg_ensemble_profile", i32, vp, i32, dp, C.POINTER(u64))
     _lib = lib
     return lib

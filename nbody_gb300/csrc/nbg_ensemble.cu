@@ -1,0 +1,622 @@
+// nbg_ensemble.cu -- many independent systems stepped together.
+//
+// No reference counterpart as a whole; it restates, per system, what the
+// reference does for one: an explicit embedded Runge-Kutta step
+// (Dormand-Prince table, nbody/nbody_solver_rkdp.cpp:30-62; the stage loop of
+// nbody/nbody_solver_rk_butcher.cpp:130-162) around the direct-sum RHS.
+// Differences, all on the device so a whole step runs without a host round
+// trip and is captured once as a CUDA graph:
+//   * every system has its own step dt_s; the embedded error
+//     e_s = dt_s * max |sum_i (b2_i - b1_i) k_i| decides accept / reject and
+//     the next dt_s = dt_s * clamp(0.9 (tol / e_s)^(1/5), 0.2, 5)
+//     (the reference compares the unscaled max |sum (b2 - b1) k| with its
+//     threshold and subdivides recursively, nbody/nbody_solver_rk_butcher.cpp:
+//     209-231; a per-system controller replaces that host-side recursion);
+//   * the accepted update is y += dt_s * sum_i b2_i k_i (the reference also
+//     advances with b2, nbody/nbody_solver_rk_butcher.cpp:233-245).
+// The RHS is the mixed-precision direct sum: FP32 pair math in packed FP32x2,
+// compensated tile sums, FP64 state.  One persistent kernel serves all
+// systems: CTAs take (system, 256-body i-block) units from an atomic counter,
+// largest systems first.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "nbg_internal.cuh"
+#include "nbg_ptx.cuh"
+#include "nbg_stats.cuh"
+
+namespace nbg {
+namespace {
+
+constexpr int kEnsThreads = 128;
+constexpr int kEnsTile = 128;
+constexpr int kStagesRK = 7;
+
+// Dormand-Prince 5(4) (nbody/nbody_solver_rkdp.cpp:30-62)
+__constant__ double c_a[kStagesRK][kStagesRK] = {
+    {0, 0, 0, 0, 0, 0, 0},
+    {1.0 / 5, 0, 0, 0, 0, 0, 0},
+    {3.0 / 40, 9.0 / 40, 0, 0, 0, 0, 0},
+    {44.0 / 45, -56.0 / 15, 32.0 / 9, 0, 0, 0, 0},
+    {19372.0 / 6561, -25360.0 / 2187, 64448.0 / 6561, -212.0 / 729, 0, 0, 0},
+    {9017.0 / 3168, -355.0 / 33, 46732.0 / 5247, 49.0 / 176, -5103.0 / 18656, 0, 0},
+    {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84, 0}};
+__constant__ double c_b1[kStagesRK] = {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192,
+                                       -2187.0 / 6784, 11.0 / 84, 0};
+__constant__ double c_b2[kStagesRK] = {5179.0 / 57600, 0, 7571.0 / 16695, 393.0 / 640,
+                                       -92097.0 / 339200, 187.0 / 2100, 1.0 / 40};
+
+struct Body2 {
+    float4 xxyy;
+    float4 zzmm;
+};
+
+struct EnsUnit {
+    int sys;
+    int i0;  // first system-local body of the block
+};
+
+struct KPtrs {
+    double* k[kStagesRK];
+};
+
+// Stage i: s = y + dt_s sum_{j<i} a_ij k_j; writes the FP32 body records of s
+// and the velocity half of k_i (= velocity of s).
+__global__ void ens_stage_kernel(int stage, const double* __restrict__ y,
+                                 const double* __restrict__ mass, const int* __restrict__ sys,
+                                 const double* __restrict__ dt, KPtrs kp, size_t B,
+                                 Body2* __restrict__ out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < B;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const double h = dt[sys[i]];
+        double s[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) s[c] = y[c * B + i];
+        for (int j = 0; j < stage; ++j) {
+            const double a = c_a[stage][j] * h;
+            if (a == 0.0) continue;
+            const double* kj = kp.k[j];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) s[c] = fma(a, kj[c * B + i], s[c]);
+        }
+        double* ki = kp.k[stage];
+        ki[i] = s[3];
+        ki[B + i] = s[4];
+        ki[2 * B + i] = s[5];
+        const float x = (float)s[0], yy = (float)s[1], z = (float)s[2], m = (float)mass[i];
+        Body2 b;
+        b.xxyy = make_float4(x, x, yy, yy);
+        b.zzmm = make_float4(z, z, m, m);
+        out[i] = b;
+    }
+}
+
+template <bool CLAMP>
+__device__ __forceinline__ void pair2e(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f2_t xi, f2_t yi,
+                                       f2_t zi, f2_t eps2, f2_t& ax, f2_t& ay, f2_t& az) {
+    const f2_t dx = f2_sub(xj, xi);
+    const f2_t dy = f2_sub(yj, yi);
+    const f2_t dz = f2_sub(zj, zi);
+    f2_t r2 = f2_fma(dz, dz, eps2);
+    r2 = f2_fma(dy, dy, r2);
+    r2 = f2_fma(dx, dx, r2);
+    float r2a, r2b;
+    f2_unpack(r2, r2a, r2b);
+    if (CLAMP) {
+        r2a = fmaxf(r2a, 1e-8f);
+        r2b = fmaxf(r2b, 1e-8f);
+    }
+    const f2_t inv = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
+    const f2_t s3 = f2_mul(f2_mul(mj, inv), f2_mul(inv, inv));
+    ax = f2_fma(dx, s3, ax);
+    ay = f2_fma(dy, s3, ay);
+    az = f2_fma(dz, s3, az);
+}
+
+// Persistent direct sum over all systems.  Each lane holds G packed pairs
+// (2G i-bodies: slots r = 0 .. 2G-1 at i0 + r * 128 + threadIdx.x).
+template <bool CLAMP, int G>
+__global__ void __launch_bounds__(kEnsThreads)
+ens_force_kernel(const Body2* __restrict__ bodies, const long long* __restrict__ off,
+                 const int* __restrict__ cnt, const EnsUnit* __restrict__ units, int nunits,
+                 unsigned* __restrict__ counter, double* __restrict__ acc, size_t B, float eps2v) {
+    __shared__ __align__(16) Body2 tile[kEnsTile];
+    __shared__ int next_unit;
+    const f2_t eps2 = f2_pack(eps2v, eps2v);
+    const f2_t zero = f2_pack(0.f, 0.f);
+    const uint32_t tbase = smem_addr(tile);
+    while (true) {
+        __syncthreads();
+        if (threadIdx.x == 0) next_unit = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int u = next_unit;
+        if (u >= nunits) break;
+        const EnsUnit un = units[u];
+        const long long o = off[un.sys];
+        const int n = cnt[un.sys];
+        f2_t xi[G], yi[G], zi[G], hx[G], hy[G], hz[G], lx[G], ly[G], lz[G];
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            const int l0 = un.i0 + (2 * g) * kEnsThreads + threadIdx.x;
+            const int l1 = l0 + kEnsThreads;
+            float x0 = 0.f, y0 = 0.f, z0 = 0.f, x1 = 0.f, y1 = 0.f, z1 = 0.f;
+            if (l0 < n) {
+                const Body2 b = bodies[o + l0];
+                x0 = b.xxyy.x; y0 = b.xxyy.z; z0 = b.zzmm.x;
+            }
+            if (l1 < n) {
+                const Body2 b = bodies[o + l1];
+                x1 = b.xxyy.x; y1 = b.xxyy.z; z1 = b.zzmm.x;
+            }
+            xi[g] = f2_pack(x0, x1);
+            yi[g] = f2_pack(y0, y1);
+            zi[g] = f2_pack(z0, z1);
+            hx[g] = hy[g] = hz[g] = lx[g] = ly[g] = lz[g] = zero;
+        }
+        for (int j0 = 0; j0 < n; j0 += kEnsTile) {
+            __syncthreads();
+            const int lj = j0 + threadIdx.x;
+            Body2 b;
+            if (lj < n) {
+                b = bodies[o + lj];
+            } else {  // zero-mass padding at the origin
+                b.xxyy = make_float4(0.f, 0.f, 0.f, 0.f);
+                b.zzmm = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            tile[threadIdx.x] = b;
+            __syncthreads();
+            f2_t ax[G], ay[G], az[G];
+#pragma unroll
+            for (int g = 0; g < G; ++g) ax[g] = ay[g] = az[g] = zero;
+            const int jn = min(kEnsTile, n - j0);
+#pragma unroll 4
+            for (int j = 0; j < jn; ++j) {
+                const float4 p0 = lds128(tbase + 32u * j);
+                const float4 p1 = lds128(tbase + 32u * j + 16u);
+                const f2_t xj = f2_pack(p0.x, p0.y), yj = f2_pack(p0.z, p0.w);
+                const f2_t zj = f2_pack(p1.x, p1.y), mj = f2_pack(p1.z, p1.w);
+#pragma unroll
+                for (int g = 0; g < G; ++g)
+                    pair2e<CLAMP>(xj, yj, zj, mj, xi[g], yi[g], zi[g], eps2, ax[g], ay[g], az[g]);
+            }
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                f2_two_sum(hx[g], lx[g], ax[g]);
+                f2_two_sum(hy[g], ly[g], ay[g]);
+                f2_two_sum(hz[g], lz[g], az[g]);
+            }
+        }
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            const int l0 = un.i0 + (2 * g) * kEnsThreads + threadIdx.x;
+            const int l1 = l0 + kEnsThreads;
+            float h0, h1, q0, q1;
+            if (l0 < n || l1 < n) {
+                const f2_t hh[3] = {hx[g], hy[g], hz[g]};
+                const f2_t ll[3] = {lx[g], ly[g], lz[g]};
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    f2_unpack(hh[c], h0, h1);
+                    f2_unpack(ll[c], q0, q1);
+                    if (l0 < n) acc[c * B + o + l0] = (double)h0 + (double)q0;
+                    if (l1 < n) acc[c * B + o + l1] = (double)h1 + (double)q1;
+                }
+            }
+        }
+    }
+}
+
+// Candidate update y_new = y + dt sum b2_i k_i and per-system error
+// max |dt sum (b2_i - b1_i) k_i| (as ordered bits, atomicMax).
+__global__ void ens_error_kernel(const double* __restrict__ y, const int* __restrict__ sys,
+                                 const double* __restrict__ dt, KPtrs kp, size_t B,
+                                 double* __restrict__ ynew, unsigned long long* __restrict__ err) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < B;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int s = sys[i];
+        const double h = dt[s];
+        double emax = 0.0;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            double acc_b2 = 0.0, acc_e = 0.0;
+#pragma unroll
+            for (int j = 0; j < kStagesRK; ++j) {
+                const double kv = kp.k[j][c * B + i];
+                acc_b2 = fma(c_b2[j], kv, acc_b2);
+                acc_e = fma(c_b2[j] - c_b1[j], kv, acc_e);
+            }
+            ynew[c * B + i] = fma(h, acc_b2, y[c * B + i]);
+            emax = fmax(emax, fabs(h * acc_e));
+        }
+        atomicMax(&err[s], (unsigned long long)__double_as_longlong(emax));
+    }
+}
+
+// One thread per system: accept / reject and the next step.
+__global__ void ens_control_kernel(int nsys, double tol, double dt_min, double dt_max,
+                                   const unsigned long long* __restrict__ err, double* __restrict__ dt,
+                                   double* __restrict__ t, unsigned* __restrict__ accepted,
+                                   unsigned* __restrict__ rejected, int* __restrict__ decision) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsys) return;
+    const double e = __longlong_as_double((long long)err[s]);
+    const double h = dt[s];
+    const bool ok = e <= tol || h <= dt_min;
+    decision[s] = ok ? 1 : 0;
+    if (ok) {
+        t[s] += h;
+        accepted[s] += 1;
+    } else {
+        rejected[s] += 1;
+    }
+    double fac = (e > 0.0) ? 0.9 * pow(tol / e, 0.2) : 5.0;
+    fac = fmin(5.0, fmax(0.2, fac));
+    dt[s] = fmin(dt_max, fmax(dt_min, h * fac));
+}
+
+__global__ void ens_commit_kernel(double* __restrict__ y, const double* __restrict__ ynew,
+                                  const int* __restrict__ sys, const int* __restrict__ decision,
+                                  size_t B) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < B;
+         i += (size_t)gridDim.x * blockDim.x) {
+        if (!decision[sys[i]]) continue;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) y[c * B + i] = ynew[c * B + i];
+    }
+}
+
+}  // namespace
+}  // namespace nbg
+
+using namespace nbg;
+
+struct nbg_ensemble {
+    nbg_engine* eng = nullptr;  // stream, error text, launch count
+    nbg_ensemble_params p{};
+    int nsys = 0;
+    size_t B = 0;
+    std::vector<long long> h_off;
+    std::vector<int> h_cnt;
+    long long* off = nullptr;
+    int* cnt = nullptr;
+    int* sys = nullptr;
+    double* y = nullptr;
+    double* ynew = nullptr;
+    double* mass = nullptr;
+    double* k[kStagesRK] = {nullptr};
+    Body2* bodies = nullptr;
+    double* dt = nullptr;
+    double* t = nullptr;
+    unsigned long long* err = nullptr;
+    unsigned* accepted = nullptr;
+    unsigned* rejected = nullptr;
+    int* decision = nullptr;
+    EnsUnit* units = nullptr;
+    int nunits = 0;
+    unsigned* counters = nullptr;  // one per stage
+    cudaGraphExec_t graph = nullptr;
+    cudaGraph_t graph_def = nullptr;
+    int G = 2;
+    unsigned force_grid = 1;
+};
+
+namespace {
+
+nbg_status ens_enqueue_step(nbg_ensemble* s) {
+    nbg_engine* e = s->eng;
+    const unsigned gv = grid_for(s->B, 256, (unsigned)e->sm_count * 8u);
+    KPtrs kp;
+    for (int i = 0; i < kStagesRK; ++i) kp.k[i] = s->k[i];
+    NBG_CUDA(e, cudaMemsetAsync(s->counters, 0, kStagesRK * sizeof(unsigned), e->stream));
+    NBG_CUDA(e, cudaMemsetAsync(s->err, 0, s->nsys * sizeof(unsigned long long), e->stream));
+    const bool clamp = !(s->p.softening > 0.0);
+    const float eps2 = (float)(s->p.softening * s->p.softening);
+    auto kern = clamp ? (s->G == 1 ? ens_force_kernel<true, 1> : ens_force_kernel<true, 2>)
+                      : (s->G == 1 ? ens_force_kernel<false, 1> : ens_force_kernel<false, 2>);
+    const unsigned grid = s->force_grid;
+    for (int st = 0; st < kStagesRK; ++st) {
+        ens_stage_kernel<<<gv, 256, 0, e->stream>>>(st, s->y, s->mass, s->sys, s->dt, kp, s->B,
+                                                    s->bodies);
+        NBG_LAUNCHED(e, "ens_stage_kernel");
+        ProfScope ps(e, NBG_K_DIRECT);
+        kern<<<grid, kEnsThreads, 0, e->stream>>>(s->bodies, s->off, s->cnt, s->units, s->nunits,
+                                                  s->counters + st, s->k[st] + 3 * s->B, s->B, eps2);
+        NBG_LAUNCHED(e, "ens_force_kernel");
+    }
+    ens_error_kernel<<<gv, 256, 0, e->stream>>>(s->y, s->sys, s->dt, kp, s->B, s->ynew, s->err);
+    NBG_LAUNCHED(e, "ens_error_kernel");
+    ens_control_kernel<<<(s->nsys + 127) / 128, 128, 0, e->stream>>>(
+        s->nsys, s->p.tolerance, s->p.dt_min, s->p.dt_max, s->err, s->dt, s->t, s->accepted,
+        s->rejected, s->decision);
+    NBG_LAUNCHED(e, "ens_control_kernel");
+    ens_commit_kernel<<<gv, 256, 0, e->stream>>>(s->y, s->ynew, s->sys, s->decision, s->B);
+    NBG_LAUNCHED(e, "ens_commit_kernel");
+    return NBG_OK;
+}
+
+void ens_free(nbg_ensemble* s) {
+    void* ptrs[] = {s->off, s->cnt, s->sys, s->y, s->ynew, s->mass, s->bodies, s->dt, s->t,
+                    s->err, s->accepted, s->rejected, s->decision, s->units, s->counters};
+    for (void* p : ptrs) cudaFree(p);
+    for (double* k : s->k) cudaFree(k);
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    if (s->graph_def) cudaGraphDestroy(s->graph_def);
+    s->graph = nullptr;
+    s->graph_def = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+void nbg_ensemble_params_default(nbg_ensemble_params* p) {
+    if (p == nullptr) return;
+    memset(p, 0, sizeof(*p));
+    p->struct_size = sizeof(nbg_ensemble_params);
+    p->device = 0;
+    p->softening = 1e-3;
+    p->tolerance = 1e-8;
+    p->dt_initial = 1e-3;
+    p->dt_min = 1e-9;
+    p->dt_max = 1e-1;
+    p->use_graph = 1;
+}
+
+nbg_status nbg_ensemble_create(const nbg_ensemble_params* p, nbg_ensemble** out) {
+    if (out == nullptr) return NBG_ERR_INVALID_ARG;
+    *out = nullptr;
+    nbg_ensemble_params prm;
+    nbg_ensemble_params_default(&prm);
+    if (p != nullptr) {
+        if (p->struct_size != sizeof(nbg_ensemble_params)) return NBG_ERR_INVALID_ARG;
+        prm = *p;
+    }
+    if (!(prm.softening >= 0.0) || !(prm.tolerance > 0.0) || !(prm.dt_initial > 0.0) ||
+        !(prm.dt_min > 0.0) || !(prm.dt_max >= prm.dt_min))
+        return NBG_ERR_INVALID_ARG;
+    nbg_params ep;
+    nbg_params_default(&ep);
+    ep.device = prm.device;
+    ep.precision = NBG_PREC_MIXED;
+    ep.softening = prm.softening;
+    nbg_engine* eng = nullptr;
+    nbg_status st = nbg_engine_create(&ep, &eng);
+    if (st != NBG_OK) return st;
+    nbg_ensemble* s = new (std::nothrow) nbg_ensemble();
+    if (s == nullptr) {
+        nbg_engine_destroy(eng);
+        return NBG_ERR_OUT_OF_MEMORY;
+    }
+    s->eng = eng;
+    s->p = prm;
+    *out = s;
+    return NBG_OK;
+}
+
+void nbg_ensemble_destroy(nbg_ensemble* s) {
+    if (s == nullptr) return;
+    cudaSetDevice(s->eng->device);
+    cudaStreamSynchronize(s->eng->stream);
+    ens_free(s);
+    nbg_engine_destroy(s->eng);
+    delete s;
+}
+
+const char* nbg_ensemble_last_error(const nbg_ensemble* s) {
+    return s == nullptr ? "" : s->eng->last_error.c_str();
+}
+
+nbg_status nbg_ensemble_init(nbg_ensemble* s, size_t nsys, const uint32_t* counts,
+                             const double* vertices, const double* velocities, const double* mass) {
+    if (s == nullptr || nsys == 0 || counts == nullptr || vertices == nullptr ||
+        velocities == nullptr || mass == nullptr)
+        return NBG_ERR_INVALID_ARG;
+    nbg_engine* e = s->eng;
+    NBG_CUDA(e, cudaSetDevice(e->device));
+    NBG_CUDA(e, cudaStreamSynchronize(e->stream));
+    ens_free(s);
+    s->nsys = (int)nsys;
+    s->h_off.assign(nsys, 0);
+    s->h_cnt.assign(nsys, 0);
+    size_t B = 0;
+    for (size_t i = 0; i < nsys; ++i) {
+        if (counts[i] == 0) return set_error(e, NBG_ERR_INVALID_ARG, "system %zu is empty", i);
+        s->h_off[i] = (long long)B;
+        s->h_cnt[i] = (int)counts[i];
+        B += counts[i];
+    }
+    s->B = B;
+    const size_t B6 = 6 * B;
+    NBG_CUDA(e, cudaMalloc(&s->off, nsys * sizeof(long long)));
+    NBG_CUDA(e, cudaMalloc(&s->cnt, nsys * sizeof(int)));
+    NBG_CUDA(e, cudaMalloc(&s->sys, B * sizeof(int)));
+    NBG_CUDA(e, cudaMalloc(&s->y, B6 * sizeof(double)));
+    NBG_CUDA(e, cudaMalloc(&s->ynew, B6 * sizeof(double)));
+    NBG_CUDA(e, cudaMalloc(&s->mass, B * sizeof(double)));
+    for (int i = 0; i < kStagesRK; ++i) NBG_CUDA(e, cudaMalloc(&s->k[i], B6 * sizeof(double)));
+    NBG_CUDA(e, cudaMalloc(&s->bodies, B * sizeof(Body2)));
+    NBG_CUDA(e, cudaMalloc(&s->dt, nsys * sizeof(double)));
+    NBG_CUDA(e, cudaMalloc(&s->t, nsys * sizeof(double)));
+    NBG_CUDA(e, cudaMalloc(&s->err, nsys * sizeof(unsigned long long)));
+    NBG_CUDA(e, cudaMalloc(&s->accepted, nsys * sizeof(unsigned)));
+    NBG_CUDA(e, cudaMalloc(&s->rejected, nsys * sizeof(unsigned)));
+    NBG_CUDA(e, cudaMalloc(&s->decision, nsys * sizeof(int)));
+    NBG_CUDA(e, cudaMalloc(&s->counters, kStagesRK * sizeof(unsigned)));
+    // host-side layout: SoA state, system ids, LPT-ordered work units
+    std::vector<double> h(B6);
+    std::vector<int> hsys(B);
+    for (size_t sI = 0; sI < nsys; ++sI)
+        for (int k = 0; k < s->h_cnt[sI]; ++k) hsys[s->h_off[sI] + k] = (int)sI;
+    for (size_t i = 0; i < B; ++i)
+        for (int d = 0; d < 3; ++d) {
+            h[d * B + i] = vertices[3 * i + d];
+            h[(3 + d) * B + i] = velocities[3 * i + d];
+        }
+    s->G = (int)std::max<int64_t>(1, std::min<int64_t>(2, e->tune_get("ensemble.pairs_per_lane", 2)));
+    const int blk = kEnsThreads * 2 * s->G;
+    std::vector<EnsUnit> units;
+    for (size_t sI = 0; sI < nsys; ++sI)
+        for (int i0 = 0; i0 < s->h_cnt[sI]; i0 += blk) units.push_back(EnsUnit{(int)sI, i0});
+    std::stable_sort(units.begin(), units.end(), [&](const EnsUnit& a, const EnsUnit& b) {
+        return s->h_cnt[a.sys] > s->h_cnt[b.sys];
+    });
+    s->nunits = (int)units.size();
+    {
+        const bool clamp = !(s->p.softening > 0.0);
+        auto kern = clamp ? (s->G == 1 ? ens_force_kernel<true, 1> : ens_force_kernel<true, 2>)
+                          : (s->G == 1 ? ens_force_kernel<false, 1> : ens_force_kernel<false, 2>);
+        int occ = 0;
+        NBG_CUDA(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kEnsThreads, 0));
+        s->force_grid = (unsigned)std::max(1, std::min(s->nunits, e->sm_count * std::max(occ, 1)));
+    }
+    NBG_CUDA(e, cudaMalloc(&s->units, units.size() * sizeof(EnsUnit)));
+    std::vector<double> dt0(nsys, s->p.dt_initial), t0(nsys, 0.0);
+    NBG_CUDA(e, cudaMemcpy(s->off, s->h_off.data(), nsys * sizeof(long long), cudaMemcpyHostToDevice));
+    NBG_CUDA(e, cudaMemcpy(s->cnt, s->h_cnt.data(), nsys * sizeof(int), cudaMemcpyHostToDevice));
+    NBG_CUDA(e, cudaMemcpy(s->sys, hsys.data(), B * sizeof(int), cudaMemcpyHostToDevice));
+    NBG_CUDA(e, cudaMemcpy(s->y, h.data(), B6 * sizeof(double), cudaMemcpyHostToDevice));
+    NBG_CUDA(e, cudaMemcpy(s->mass, mass, B * sizeof(double), cudaMemcpyHostToDevice));
+    NBG_CUDA(e, cudaMemcpy(s->units, units.data(), units.size() * sizeof(EnsUnit),
+                           cudaMemcpyHostToDevice));
+    NBG_CUDA(e, cudaMemcpy(s->dt, dt0.data(), nsys * sizeof(double), cudaMemcpyHostToDevice));
+    NBG_CUDA(e, cudaMemcpy(s->t, t0.data(), nsys * sizeof(double), cudaMemcpyHostToDevice));
+    NBG_CUDA(e, cudaMemset(s->accepted, 0, nsys * sizeof(unsigned)));
+    NBG_CUDA(e, cudaMemset(s->rejected, 0, nsys * sizeof(unsigned)));
+    return NBG_OK;
+}
+
+nbg_status nbg_ensemble_step(nbg_ensemble* s, int steps) {
+    if (s == nullptr || steps < 0) return NBG_ERR_INVALID_ARG;
+    if (s->B == 0) return set_error(s->eng, NBG_ERR_NOT_INITIALIZED, "ensemble not initialised");
+    nbg_engine* e = s->eng;
+    NBG_CUDA(e, cudaSetDevice(e->device));
+    if (!s->p.use_graph) {
+        for (int k = 0; k < steps; ++k) {
+            nbg_status st = ens_enqueue_step(s);
+            if (st != NBG_OK) return st;
+        }
+        return NBG_OK;
+    }
+    if (s->graph == nullptr) {
+        // capture one whole RK step (stage combinations, forces, error,
+        // control, commit) once; later steps replay it
+        const bool prof = e->profiling;
+        e->profiling = false;  // no host-side event bookkeeping inside the capture
+        NBG_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+        const uint64_t l0 = e->launches;
+        nbg_status st = ens_enqueue_step(s);
+        cudaGraph_t g = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+        e->profiling = prof;
+        if (st != NBG_OK) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (ce != cudaSuccess) return cuda_error(e, ce, "cudaStreamEndCapture");
+        s->graph_def = g;
+        NBG_CUDA(e, cudaGraphInstantiate(&s->graph, g, 0));
+        e->launches = l0;  // captured, not launched
+    }
+    const uint64_t per_step = 3 + 2 * kStagesRK;
+    for (int k = 0; k < steps; ++k) {
+        ProfScope ps(e, NBG_K_ENS_STEP);
+        NBG_CUDA(e, cudaGraphLaunch(s->graph, e->stream));
+        e->launches += per_step;
+    }
+    return NBG_OK;
+}
+
+nbg_status nbg_ensemble_synchronize(nbg_ensemble* s) {
+    if (s == nullptr) return NBG_ERR_INVALID_ARG;
+    return nbg_synchronize(s->eng);
+}
+
+nbg_status nbg_ensemble_status(nbg_ensemble* s, double* t, double* dt, uint32_t* accepted,
+                               uint32_t* rejected) {
+    if (s == nullptr) return NBG_ERR_INVALID_ARG;
+    nbg_engine* e = s->eng;
+    NBG_CUDA(e, cudaStreamSynchronize(e->stream));
+    if (t) NBG_CUDA(e, cudaMemcpy(t, s->t, s->nsys * sizeof(double), cudaMemcpyDeviceToHost));
+    if (dt) NBG_CUDA(e, cudaMemcpy(dt, s->dt, s->nsys * sizeof(double), cudaMemcpyDeviceToHost));
+    if (accepted)
+        NBG_CUDA(e, cudaMemcpy(accepted, s->accepted, s->nsys * sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (rejected)
+        NBG_CUDA(e, cudaMemcpy(rejected, s->rejected, s->nsys * sizeof(unsigned), cudaMemcpyDeviceToHost));
+    return NBG_OK;
+}
+
+nbg_status nbg_ensemble_get_state(nbg_ensemble* s, double* vertices, double* velocities) {
+    if (s == nullptr || vertices == nullptr || velocities == nullptr) return NBG_ERR_INVALID_ARG;
+    nbg_engine* e = s->eng;
+    std::vector<double> h(6 * s->B);
+    NBG_CUDA(e, cudaStreamSynchronize(e->stream));
+    NBG_CUDA(e, cudaMemcpy(h.data(), s->y, 6 * s->B * sizeof(double), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < s->B; ++i)
+        for (int d = 0; d < 3; ++d) {
+            vertices[3 * i + d] = h[d * s->B + i];
+            velocities[3 * i + d] = h[(3 + d) * s->B + i];
+        }
+    return NBG_OK;
+}
+
+nbg_status nbg_ensemble_fcompute(nbg_ensemble* s, double* f) {
+    if (s == nullptr || f == nullptr) return NBG_ERR_INVALID_ARG;
+    nbg_engine* e = s->eng;
+    if (s->B == 0) return set_error(e, NBG_ERR_NOT_INITIALIZED, "ensemble not initialised");
+    // stage 0 of a step: k_0 = [v ; a(y)] of the current state
+    KPtrs kp;
+    for (int i = 0; i < kStagesRK; ++i) kp.k[i] = s->k[i];
+    const unsigned gv = grid_for(s->B, 256, (unsigned)e->sm_count * 8u);
+    NBG_CUDA(e, cudaMemsetAsync(s->counters, 0, sizeof(unsigned), e->stream));
+    ens_stage_kernel<<<gv, 256, 0, e->stream>>>(0, s->y, s->mass, s->sys, s->dt, kp, s->B, s->bodies);
+    NBG_LAUNCHED(e, "ens_stage_kernel");
+    const bool clamp = !(s->p.softening > 0.0);
+    auto kern = clamp ? (s->G == 1 ? ens_force_kernel<true, 1> : ens_force_kernel<true, 2>)
+                      : (s->G == 1 ? ens_force_kernel<false, 1> : ens_force_kernel<false, 2>);
+    kern<<<s->force_grid, kEnsThreads, 0, e->stream>>>(
+        s->bodies, s->off, s->cnt, s->units, s->nunits, s->counters, s->k[0] + 3 * s->B, s->B,
+        (float)(s->p.softening * s->p.softening));
+    NBG_LAUNCHED(e, "ens_force_kernel");
+    NBG_CUDA(e, cudaStreamSynchronize(e->stream));
+    NBG_CUDA(e, cudaMemcpy(f, s->k[0], 6 * s->B * sizeof(double), cudaMemcpyDeviceToHost));
+    return NBG_OK;
+}
+
+nbg_status nbg_ensemble_statistics(nbg_ensemble* s, double* out) {
+    if (s == nullptr || out == nullptr) return NBG_ERR_INVALID_ARG;
+    nbg_engine* e = s->eng;
+    double* d_out = nullptr;
+    NBG_CUDA(e, cudaMalloc(&d_out, 12 * (size_t)s->nsys * sizeof(double)));
+    nbg_status st = stats_segments(e, s->y, s->mass, s->B, s->nsys, s->off, s->cnt,
+                                   s->h_off.data(), s->h_cnt.data(),
+                                   s->p.softening * s->p.softening, d_out);
+    if (st == NBG_OK)
+        NBG_CUDA(e, cudaMemcpy(out, d_out, 12 * (size_t)s->nsys * sizeof(double),
+                               cudaMemcpyDeviceToHost));
+    cudaFree(d_out);
+    return st;
+}
+
+nbg_status nbg_ensemble_tune_set(nbg_ensemble* s, const char* key, int64_t value) {
+    if (s == nullptr) return NBG_ERR_INVALID_ARG;
+    return nbg_tune_set(s->eng, key, value);
+}
+
+uint64_t nbg_ensemble_launch_count(const nbg_ensemble* s) {
+    return s == nullptr ? 0 : s->eng->launches;
+}
+
+nbg_status nbg_ensemble_profile(nbg_ensemble* s, int enable, double* force_ms,
+                                uint64_t* force_launches) {
+    if (s == nullptr) return NBG_ERR_INVALID_ARG;
+    if (force_ms != nullptr || force_launches != nullptr) {
+        nbg_status st = nbg_profile_query(s->eng, NBG_K_DIRECT, force_ms, force_launches);
+        if (st != NBG_OK) return st;
+    }
+    return nbg_profile_enable(s->eng, enable);
+}
+
+}  // extern "C"

@@ -1,0 +1,186 @@
+// nbg_stats.cu -- conservation checks on the GPU (FP64).
+//
+// The reference computes momentum P, angular momentum L, kinetic and
+// potential energy E and the mass centre V on the host with Kahan sums,
+// including an O(N^2) single-threaded potential-energy loop
+// (nbody/nbody_data.cpp:57-145, nbody/summation_proxy.h).  Here the same
+// quantities come from FP64 reductions on the device, for one system or for
+// every system of an ensemble (segments of a concatenated body array).
+// Per system the 12 outputs are P[3], L[3], KE, PE, centre[3], mass; KE and
+// PE are halved as print_statistics does, and pairs closer than the
+// reference's MinDistance contribute no potential (nbody/nbody_data.cpp:46-55).
+// With a Plummer softening eps the pair potential is -m_i m_j / sqrt(r^2 + eps^2),
+// the potential of the softened force the engine integrates; eps = 0 is the
+// reference's form.
+#include "nbg_internal.cuh"
+#include "nbg_stats.cuh"
+
+namespace nbg {
+namespace {
+
+constexpr int kStatThreads = 256;
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x < 32) {
+        r = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    }
+    return r;  // valid in thread 0
+}
+
+// One CTA per system: the O(N) sums.
+__global__ void __launch_bounds__(kStatThreads)
+stats_linear_kernel(const double* __restrict__ y, const double* __restrict__ mass, size_t stride,
+                    const long long* __restrict__ off, const int* __restrict__ cnt,
+                    double* __restrict__ out) {
+    __shared__ double sh[kStatThreads / 32];
+    const int s = blockIdx.x;
+    const long long o = off[s];
+    const int n = cnt[s];
+    double acc[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const size_t i = (size_t)(o + k);
+        const double m = mass[i];
+        const double rx = y[i], ry = y[stride + i], rz = y[2 * stride + i];
+        const double px = y[3 * stride + i] * m, py = y[4 * stride + i] * m, pz = y[5 * stride + i] * m;
+        acc[0] += px;
+        acc[1] += py;
+        acc[2] += pz;
+        acc[3] += ry * pz - rz * py;
+        acc[4] += rz * px - rx * pz;
+        acc[5] += rx * py - ry * px;
+        acc[6] += (y[3 * stride + i] * y[3 * stride + i] + y[4 * stride + i] * y[4 * stride + i] +
+                   y[5 * stride + i] * y[5 * stride + i]) * m;
+        acc[7] += rx * m;
+        acc[8] += ry * m;
+        acc[9] += rz * m;
+        acc[10] += m;
+    }
+    double res[11];
+    for (int q = 0; q < 11; ++q) res[q] = block_sum(acc[q], sh);
+    if (threadIdx.x == 0) {
+        double* r = out + 12 * (size_t)s;
+        r[0] = res[0];
+        r[1] = res[1];
+        r[2] = res[2];
+        r[3] = res[3];
+        r[4] = res[4];
+        r[5] = res[5];
+        r[6] = res[6] / 2;
+        r[8] = res[7] / res[10];
+        r[9] = res[8] / res[10];
+        r[10] = res[9] / res[10];
+        r[11] = res[10];
+    }
+}
+
+struct PairUnit {
+    int sys;
+    int i0;  // first body (system-local) of the 256-body block
+};
+
+// Potential energy: one CTA per (system, 256 i-bodies); FP64 pair sums over
+// j-tiles in shared memory; one atomicAdd per CTA into PE[s] (pre-halved).
+__global__ void __launch_bounds__(kStatThreads)
+stats_potential_kernel(const double* __restrict__ y, const double* __restrict__ mass, size_t stride,
+                       const long long* __restrict__ off, const int* __restrict__ cnt,
+                       const PairUnit* __restrict__ units, double eps2,
+                       double* __restrict__ out) {
+    __shared__ double tx[kStatThreads], ty[kStatThreads], tz[kStatThreads], tm[kStatThreads];
+    __shared__ double sh[kStatThreads / 32];
+    const PairUnit u = units[blockIdx.x];
+    const long long o = off[u.sys];
+    const int n = cnt[u.sys];
+    const int li = u.i0 + threadIdx.x;
+    const bool live = li < n;
+    const size_t i = (size_t)(o + (live ? li : 0));
+    const double xi = y[i], yi = y[stride + i], zi = y[2 * stride + i], mi = live ? mass[i] : 0.0;
+    double pe = 0.0;
+    for (int j0 = 0; j0 < n; j0 += kStatThreads) {
+        const int lj = j0 + threadIdx.x;
+        __syncthreads();
+        if (lj < n) {
+            const size_t j = (size_t)(o + lj);
+            tx[threadIdx.x] = y[j];
+            ty[threadIdx.x] = y[stride + j];
+            tz[threadIdx.x] = y[2 * stride + j];
+            tm[threadIdx.x] = mass[j];
+        }
+        __syncthreads();
+        const int c = min(kStatThreads, n - j0);
+        for (int k = 0; k < c; ++k) {
+            if (j0 + k == li) continue;
+            const double dx = xi - tx[k], dy = yi - ty[k], dz = zi - tz[k];
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            if (eps2 == 0.0 && r2 < kMinDistance) continue;
+            pe -= tm[k] / sqrt(r2 + eps2);
+        }
+    }
+    const double tot = block_sum(pe * mi, sh);
+    if (threadIdx.x == 0) atomicAdd(out + 12 * (size_t)u.sys + 7, tot / 2);
+}
+
+}  // namespace
+
+nbg_status stats_segments(nbg_engine* e, const double* y, const double* mass, size_t stride,
+                          int nsys, const long long* d_off, const int* d_cnt,
+                          const long long* h_off, const int* h_cnt, double eps2,
+                          double* d_out) {
+    std::vector<PairUnit> units;
+    for (int s = 0; s < nsys; ++s)
+        for (int i0 = 0; i0 < h_cnt[s]; i0 += kStatThreads) units.push_back(PairUnit{s, i0});
+    (void)h_off;
+    PairUnit* d_units = nullptr;
+    NBG_CUDA(e, cudaMalloc(&d_units, units.size() * sizeof(PairUnit) + 16));
+    NBG_CUDA(e, cudaMemcpyAsync(d_units, units.data(), units.size() * sizeof(PairUnit),
+                                cudaMemcpyHostToDevice, e->stream));
+    NBG_CUDA(e, cudaMemsetAsync(d_out, 0, 12 * (size_t)nsys * sizeof(double), e->stream));
+    stats_linear_kernel<<<nsys, kStatThreads, 0, e->stream>>>(y, mass, stride, d_off, d_cnt, d_out);
+    NBG_LAUNCHED(e, "stats_linear_kernel");
+    if (!units.empty()) {
+        stats_potential_kernel<<<(unsigned)units.size(), kStatThreads, 0, e->stream>>>(
+            y, mass, stride, d_off, d_cnt, d_units, eps2, d_out);
+        NBG_LAUNCHED(e, "stats_potential_kernel");
+    }
+    NBG_CUDA(e, cudaStreamSynchronize(e->stream));
+    cudaFree(d_units);
+    return NBG_OK;
+}
+
+}  // namespace nbg
+
+extern "C" nbg_status nbg_statistics(nbg_engine* e, const nbg_buffer* y, double out[12]) {
+    using namespace nbg;
+    if (e == nullptr || out == nullptr) return NBG_ERR_INVALID_ARG;
+    if (y == nullptr || e->buffers.count(y) == 0)
+        return set_error(e, NBG_ERR_FOREIGN_BUFFER, "y is not gb300 memory");
+    if (e->count == 0) return set_error(e, NBG_ERR_NOT_INITIALIZED, "engine not initialized");
+    if (y->bytes < 6 * e->count * sizeof(double))
+        return set_error(e, NBG_ERR_SIZE_MISMATCH, "y smaller than 6N doubles");
+    long long h_off = 0;
+    int h_cnt = (int)e->count;
+    long long* d_off = nullptr;
+    int* d_cnt = nullptr;
+    double* d_out = nullptr;
+    NBG_CUDA(e, cudaMalloc(&d_off, sizeof(long long)));
+    NBG_CUDA(e, cudaMalloc(&d_cnt, sizeof(int)));
+    NBG_CUDA(e, cudaMalloc(&d_out, 12 * sizeof(double)));
+    NBG_CUDA(e, cudaMemcpyAsync(d_off, &h_off, sizeof(h_off), cudaMemcpyHostToDevice, e->stream));
+    NBG_CUDA(e, cudaMemcpyAsync(d_cnt, &h_cnt, sizeof(h_cnt), cudaMemcpyHostToDevice, e->stream));
+    nbg_status s = stats_segments(e, static_cast<const double*>(y->dptr), e->d_mass, e->count, 1,
+                                  d_off, d_cnt, &h_off, &h_cnt,
+                                  e->params.softening * e->params.softening, d_out);
+    if (s == NBG_OK) {
+        NBG_CUDA(e, cudaMemcpy(out, d_out, 12 * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    cudaFree(d_off);
+    cudaFree(d_cnt);
+    cudaFree(d_out);
+    return s;
+}

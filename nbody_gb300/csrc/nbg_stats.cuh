@@ -1,0 +1,18 @@
+// nbg_stats.cuh -- FP64 conservation sums over segments of a body array.
+#pragma once
+
+#include <vector>
+
+#include "nbg_internal.cuh"
+
+namespace nbg {
+
+// Systems s = 0..nsys-1 occupy bodies [off[s], off[s] + cnt[s]) of SoA state
+// y with the given stride.  d_out receives 12 doubles per system; eps2 is
+// the softening of the pair potential (0 = the reference's potential).
+nbg_status stats_segments(nbg_engine* e, const double* y, const double* mass, size_t stride,
+                          int nsys, const long long* d_off, const int* d_cnt,
+                          const long long* h_off, const int* h_cnt, double eps2,
+                          double* d_out);
+
+}  // namespace nbg

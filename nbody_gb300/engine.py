@@ -421,6 +421,17 @@ class NbodyEngineGB300:
         self._check(self._lib.nbg_measure_fp32_peak(self._h, C.byref(r)), "measure_fp32_peak")
         return r.value
 
+    def statistics(self, y: Optional[Memory] = None) -> np.ndarray:
+        """P[3], L[3], KE, PE, mass centre[3], mass of state y (default: get_y()),
+        FP64 on the GPU (nbody/nbody_data.cpp:57-145)."""
+        hy = self._mem(y if y is not None else self._y, "y")
+        out = np.zeros(12)
+        if hy is not None:
+            self._check(self._lib.nbg_statistics(self._h, hy,
+                                                 out.ctypes.data_as(C.POINTER(C.c_double))),
+                        "statistics")
+        return out
+
     def bh_counters(self):
         """(node visits, interactions) of the mixed Barnes-Hut walk since the last call."""
         v = C.c_uint64(0)

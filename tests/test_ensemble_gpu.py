@@ -1,0 +1,120 @@
+"""Batched ensemble: per-system forces against the oracle, one fixed-step
+rkdp step against the oracle's restatement of the reference Butcher driver,
+graph replay equal to direct launches, and adaptive runs that conserve
+energy."""
+import numpy as np
+import pytest
+
+from nbody_gb300.data import NBodyData
+from nbody_gb300.ensemble import Ensemble
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [1, 33, 64, 100, 257, 1000, 4096]
+
+
+def _systems(sizes, seed=0, kind="plummer"):
+    out = []
+    for i, n in enumerate(sizes):
+        if kind == "plummer" and n > 1:
+            out.append(NBodyData.plummer(n, seed=seed + i))
+        else:
+            out.append(NBodyData.uniform_cube(n, side=2.0, seed=seed + i))
+    return out
+
+
+@pytest.mark.parametrize("eps", [1e-3, 0.0])
+def test_ensemble_forces_vs_oracle(gpulib, oracle, eps):
+    sy = _systems(SIZES, seed=3)
+    ens = Ensemble(softening=eps)
+    ens.init(sy)
+    f = ens.fcompute()
+    B = sum(SIZES)
+    a = f[3 * B:].reshape(3, B).T
+    off = 0
+    for d in sy:
+        n = d.get_count()
+        ref = oracle.accel_rows(d.to_state(), d.mass, eps)
+        got = a[off:off + n]
+        assert np.array_equal(f[off:off + n], d.velocities[:, 0])
+        if n > 1:
+            rel = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+            assert np.sqrt(np.mean(rel ** 2)) < 1e-5, (n, rel.max())
+        else:
+            assert np.all(got == 0.0)
+        off += n
+    ens.close()
+
+
+def test_fixed_step_matches_oracle_rkdp(gpulib, oracle):
+    """dt_min = dt_max: every attempt is accepted with y += dt sum b2 k; the
+    oracle's rkdp with max_recursion 0 does the same step (reference clamp,
+    no softening)."""
+    dt = 1e-3
+    sy = _systems([64, 200, 1000], seed=5)
+    ens = Ensemble(softening=0.0, tolerance=1e-30, dt_initial=dt, dt_min=dt, dt_max=dt)
+    ens.init(sy)
+    ens.step(1)
+    v, u = ens.get_state()
+    off = 0
+    for d in sy:
+        n = d.get_count()
+        yref, _, _ = oracle.solver_run("rkdp", d.to_state(), d.mass, 0.5 * dt, dt, dt,
+                                       max_recursion=0)
+        pos = yref[:3 * n].reshape(3, n).T
+        vel = yref[3 * n:].reshape(3, n).T
+        # FP32 pair math: the step's change agrees to ~1e-5 of its size
+        dv = np.max(np.abs(vel - d.velocities))
+        dx = np.max(np.abs(pos - d.vertices))
+        assert np.max(np.abs(u[off:off + n] - vel)) <= 2e-4 * dv
+        assert np.max(np.abs(v[off:off + n] - pos)) <= 2e-4 * dx
+        off += n
+    t, dts, acc, rej = ens.status()
+    assert np.all(acc == 1) and np.all(rej == 0) and np.allclose(t, dt)
+    ens.close()
+
+
+def test_graph_equals_direct_launches(gpulib):
+    sy = _systems([64, 300, 1500], seed=8)
+    res = []
+    for use_graph in (True, False):
+        ens = Ensemble(tolerance=1e-8, use_graph=use_graph)
+        ens.init(sy)
+        ens.step(5)
+        res.append(ens.get_state())
+        res.append(ens.status())
+        ens.close()
+    assert np.array_equal(res[0][0], res[2][0]) and np.array_equal(res[0][1], res[2][1])
+    for a, b in zip(res[1], res[3]):
+        assert np.array_equal(a, b)
+
+
+def test_adaptive_energy_drift(gpulib, oracle):
+    rng = np.random.default_rng(2)
+    sizes = rng.integers(64, 2049, size=24).tolist()
+    sy = _systems(sizes, seed=11)
+    ens = Ensemble(tolerance=1e-8)
+    ens.init(sy)
+    st0 = ens.statistics()
+    ens.step(20)
+    st1 = ens.statistics()
+    t, dt, acc, rej = ens.status()
+    e0, e1 = st0[:, 6] + st0[:, 7], st1[:, 6] + st1[:, 7]
+    drift = np.abs((e1 - e0) / e0)
+    print(f"\nensemble: accepted {acc.sum()} rejected {rej.sum()} max drift {drift.max():.2e} "
+          f"median t {np.median(t):.3f}")
+    assert np.all(acc + rej == 20)
+    assert np.all(acc > 0)
+    assert drift.max() < 1e-5
+    ens.close()
+
+
+def test_ensemble_statistics_unsoftened_match_oracle(gpulib, oracle):
+    sy = _systems([64, 500, 1200], seed=13)
+    ens = Ensemble(softening=0.0)
+    ens.init(sy)
+    st = ens.statistics()
+    for k, d in enumerate(sy):
+        ref = oracle.statistics(d.to_state(), d.mass)
+        assert np.allclose(st[k], ref, rtol=1e-10, atol=1e-13)
+    ens.close()
