@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N_BODIES)
     ap.add_argument("--no-bh", action="store_true", help="skip the Barnes-Hut measurements")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble measurements")
+    ap.add_argument("--bh-only", action="store_true",
+                    help="run only the Barnes-Hut suite (with --bh-n bodies); prints its JSON")
+    ap.add_argument("--bh-n", type=int, default=1 << 20, help="bodies of the Barnes-Hut suite")
     return ap.parse_args()
 
 
@@ -247,21 +251,60 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
             "warp_node_visits_per_warp": visits / calls / (n_bh / 32)}
 
 
-def run_bh_suite(rank: int):
+def run_bh_suite(rank: int, n_bh: int = 1 << 20):
     """Plummer N = 2^20, softening 1e-3, heap_stackless, rebuilt every fcompute."""
     from nbody_gb300.data import NBodyData
     from oracle.oracle import load_oracle
-    n_bh = 1 << 20
     d = NBodyData.plummer(n_bh, seed=3)
     y = d.to_state()
     rows = np.random.default_rng(7).choice(n_bh, size=4096, replace=False)
     a_ref = load_oracle().accel_rows(y, d.mass, SOFTENING, rows=rows)
-    res = {"workload": "Barnes-Hut fcompute, N=1048576 Plummer, softening 1e-3, heap_stackless, "
+    res = {"workload": f"Barnes-Hut fcompute, N={n_bh} Plummer, softening 1e-3, heap_stackless, "
                        "tree rebuilt every call, FP32 walk / FP64 state",
            "error_judge": "FP64 direct sum (oracle) on 4096 sampled bodies"}
     res["plain_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d)
     res["plain_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d)
     return res
+
+
+def run_ensemble_suite(steps: int = 20):
+    """2048 Plummer clusters, N_s ~ U{64..4096} (seeded), softening 1e-3,
+    rkdp per-system control (tolerance 1e-8), one graph per step."""
+    from nbody_gb300.data import NBodyData
+    from nbody_gb300.ensemble import Ensemble
+    rng = np.random.default_rng(2024)
+    sizes = rng.integers(64, 4097, size=2048)
+    systems = [NBodyData.plummer(int(n), seed=100 + i) for i, n in enumerate(sizes)]
+    ens = Ensemble(softening=SOFTENING, tolerance=1e-8, dt_initial=1e-3)
+    ens.init(systems)
+    st0 = ens.statistics()
+    ens.step(1)  # warm-up (captures the graph)
+    ens.synchronize()
+    _, _, acc0, rej0 = ens.status()
+    import torch
+    ens.profile(True)
+    t0 = time.perf_counter()
+    ens.step(steps)
+    ens.synchronize()
+    wall = time.perf_counter() - t0
+    fms, flaunch = ens.profile(False)
+    t, dt, acc, rej = ens.status()
+    st1 = ens.statistics()
+    e0, e1 = st0[:, 6] + st0[:, 7], st1[:, 6] + st1[:, 7]
+    drift = np.abs((e1 - e0) / e0)
+    accepted = int((acc - acc0).sum())
+    pairs = float((sizes.astype(np.float64) ** 2).sum()) * 7 * steps
+    ens.close()
+    return {"workload": "2048 Plummer clusters, N_s uniform in [64, 4096], softening 1e-3, "
+                        "rkdp per-system adaptive (tolerance 1e-8), graph per step",
+            "bodies": int(sizes.sum()), "steps": steps,
+            "system_steps_per_s": 2048 * steps / wall,
+            "accepted_system_steps_per_s": accepted / wall,
+            "accepted_fraction": accepted / (2048 * steps),
+            "ms_per_step": wall / steps * 1e3,
+            "pairs_per_s": pairs / wall,
+            "energy_drift_median": float(np.median(drift)),
+            "energy_drift_max": float(drift.max())}
 
 
 def run_gb300(args):
@@ -372,7 +415,8 @@ def run_gb300(args):
         cpu = {"value": v, "unit": "pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
                "sample": f"block engine (FP64) on {rows} of {n} rows x {n} bodies, {dt:.1f} s"}
 
-    bh = run_bh_suite(rank) if (rank == 0 and not args.no_bh) else None
+    bh = run_bh_suite(rank, args.bh_n) if (rank == 0 and not args.no_bh) else None
+    ensemble = run_ensemble_suite() if (rank == 0 and not args.no_ensemble) else None
 
     if rank == 0:
         line = {
@@ -402,6 +446,7 @@ def run_gb300(args):
             "clocks": clk,
             "force_error": err,
             "bh": bh,
+            "ensemble": ensemble,
             "wall_s_timed": wall,
         }
         print(json.dumps(line), flush=True)
@@ -414,6 +459,9 @@ def run_gb300(args):
 
 def main():
     args = parse()
+    if args.bh_only:
+        print(json.dumps(run_bh_suite(0, args.bh_n)), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
