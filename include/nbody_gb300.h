@@ -222,7 +222,9 @@ uint64_t nbg_launch_count(const nbg_engine* e);
 /* Tuning knobs (set by the autotuner or by hand; no reference counterpart).
  * Keys: "direct.pairs_per_lane" (2 or 4 packed i-pairs per lane),
  *       "direct.unroll" (2, 4 or 8: j-loop unroll),
- *       "direct.blocks_per_sm" (CTAs per SM of the persistent direct grid). */
+ *       "direct.blocks_per_sm" (CTAs per SM of the persistent direct grid),
+ *       "bh.walk" (1: group walk with interaction lists, 0: warp-coherent
+ *       stackless walk) for the mixed-precision Barnes-Hut path. */
 nbg_status nbg_tune_set(nbg_engine* e, const char* key, int64_t value);
 nbg_status nbg_tune_get(nbg_engine* e, const char* key, int64_t* value);
 

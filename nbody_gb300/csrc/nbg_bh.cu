@@ -149,6 +149,197 @@ bh_walk_mixed_kernel(const double* __restrict__ y, double* __restrict__ f, int n
     }
 }
 
+// ---------------------------------------------------------------------------
+// group walk: 32 nodes tested per warp step, interactions evaluated in batches
+// ---------------------------------------------------------------------------
+// A warp owns 32 consecutive leaves (a compact kd subtree).  It walks the heap
+// breadth-first-by-32: each step pops up to 32 candidate nodes from a warp
+// stack in shared memory, one per lane, and tests each against the bounding
+// box of the 32 bodies: a node is accepted when the box's nearest point is
+// outside the node's critical radius (then every body of the group accepts
+// it); leaves are always accepted (a body meets itself at distance 0, which
+// contributes nothing); other nodes are opened and their two children pushed.
+// Accepted nodes go to an interaction list, stored pairwise as
+// (x x | y y | z z | m m) records so one LDS.128 feeds FP32x2 operands, and
+// every lane evaluates the list for its own body with the direct-sum pair
+// kernel.  Each body's accepted set refines its per-body set (box distance
+// <= body distance), so the result is at least as accurate as the
+// reference's per-body walk at the same ratio.
+constexpr int kGWWarps = 4;
+constexpr int kGWThreads = kGWWarps * 32;
+constexpr int kGWStack = 1536;  // node indices per warp
+constexpr int kGWList = 256;    // interaction entries per warp (128 records)
+
+struct PairRec {
+    float x[2], y[2], z[2], m[2];
+};
+
+struct GroupSmem {
+    int stack[kGWWarps][kGWStack];
+    PairRec list[kGWWarps][kGWList / 2];
+};
+
+template <bool CLAMP>
+__device__ __forceinline__ void group_pair(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f2_t xi, f2_t yi,
+                                           f2_t zi, f2_t eps2, f2_t& ax, f2_t& ay, f2_t& az) {
+    const f2_t dx = f2_sub(xj, xi);
+    const f2_t dy = f2_sub(yj, yi);
+    const f2_t dz = f2_sub(zj, zi);
+    f2_t r2 = f2_fma(dz, dz, eps2);
+    r2 = f2_fma(dy, dy, r2);
+    r2 = f2_fma(dx, dx, r2);
+    float r2a, r2b;
+    f2_unpack(r2, r2a, r2b);
+    if (CLAMP) {
+        r2a = fmaxf(r2a, 1e-8f);
+        r2b = fmaxf(r2b, 1e-8f);
+    }
+    const f2_t inv = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
+    const f2_t s3 = f2_mul(f2_mul(mj, inv), f2_mul(inv, inv));
+    ax = f2_fma(dx, s3, ax);
+    ay = f2_fma(dy, s3, ay);
+    az = f2_fma(dz, s3, az);
+}
+
+template <bool CLAMP>
+__global__ void __launch_bounds__(kGWThreads)
+bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n, float eps2v,
+                     TreeState t, unsigned* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    GroupSmem& S = *reinterpret_cast<GroupSmem*>(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * kGWWarps + warp;
+    if (gw * 32 >= n) return;
+    const int tid = gw * 32 + lane;
+    const bool live = tid < n;
+    const int leaf = n + (live ? tid : gw * 32);
+    const float4 me = __ldg(&t.node4[leaf]);
+    // bounding box of the group
+    float lo[3] = {me.x, me.y, me.z}, hi[3] = {me.x, me.y, me.z};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+    int* stack = S.stack[warp];
+    PairRec* list = S.list[warp];
+    const uint32_t list_addr = smem_addr(list);
+    const f2_t eps2 = f2_pack(eps2v, eps2v);
+    const f2_t zero = f2_pack(0.f, 0.f);
+    const f2_t xi = f2_pack(me.x, me.x), yi = f2_pack(me.y, me.y), zi = f2_pack(me.z, me.z);
+    f2_t hx = zero, hy = zero, hz = zero, lx = zero, ly = zero, lz = zero;
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned long long tests = 0, inter = 0;
+    if (lane == 0) stack[0] = 1;
+    __syncwarp();
+    int sp = 1, lc = 0;
+    bool overflow = false;
+
+    auto evaluate = [&]() {
+        if (lc & 1) {  // pad to whole records with a massless entry
+            if (lane == 0) {
+                PairRec& r = list[lc >> 1];
+                r.x[1] = 0.f;
+                r.y[1] = 0.f;
+                r.z[1] = 0.f;
+                r.m[1] = 0.f;
+            }
+            __syncwarp();
+        }
+        f2_t ax = zero, ay = zero, az = zero;
+        const int recs = (lc + 1) >> 1;
+#pragma unroll 4
+        for (int r = 0; r < recs; ++r) {
+            const float4 p0 = lds128(list_addr + 32u * r);
+            const float4 p1 = lds128(list_addr + 32u * r + 16u);
+            group_pair<CLAMP>(f2_pack(p0.x, p0.y), f2_pack(p0.z, p0.w), f2_pack(p1.x, p1.y),
+                              f2_pack(p1.z, p1.w), xi, yi, zi, eps2, ax, ay, az);
+        }
+        f2_two_sum(hx, lx, ax);
+        f2_two_sum(hy, ly, ay);
+        f2_two_sum(hz, lz, az);
+        inter += (unsigned long long)lc;
+        lc = 0;
+        __syncwarp();
+    };
+
+    while (sp > 0) {
+        const int k = min(sp, 32);
+        const bool valid = lane < k;
+        int c = 0;
+        if (valid) c = stack[sp - 1 - lane];
+        __syncwarp();
+        sp -= k;
+        tests += (unsigned long long)k;
+        bool accept = false, open = false;
+        float4 nd = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (valid) {
+            nd = __ldg(&t.node4[c]);
+            if (c >= n) {
+                accept = true;
+            } else {
+                const float ex = fmaxf(fmaxf(lo[0] - nd.x, nd.x - hi[0]), 0.f);
+                const float ey = fmaxf(fmaxf(lo[1] - nd.y, nd.y - hi[1]), 0.f);
+                const float ez = fmaxf(fmaxf(lo[2] - nd.z, nd.z - hi[2]), 0.f);
+                const float dmin2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+                accept = dmin2 > nd.w;
+                open = !accept;
+            }
+        }
+        const unsigned am = __ballot_sync(0xffffffffu, accept);
+        const unsigned om = __ballot_sync(0xffffffffu, open);
+        if (accept) {
+            const int q = lc + __popc(am & lt);
+            PairRec& r = list[q >> 1];
+            const int h = q & 1;
+            r.x[h] = nd.x;
+            r.y[h] = nd.y;
+            r.z[h] = nd.z;
+            r.m[h] = __ldg(&t.nodem[c]);
+        }
+        lc += __popc(am);
+        const int npush = 2 * __popc(om);
+        if (sp + npush > kGWStack) {  // cannot happen for heaps below 2^40 nodes
+            overflow = true;
+            break;
+        }
+        if (open) {
+            const int q = sp + 2 * __popc(om & lt);
+            stack[q] = 2 * c + 1;
+            stack[q + 1] = 2 * c;
+        }
+        sp += npush;
+        __syncwarp();
+        if (lc > kGWList - 32) evaluate();
+    }
+    if (overflow) {
+        if (lane == 0) atomicOr(err, kDevErrWalkOverflow);
+    }
+    if (lc > 0) evaluate();
+    if (live) {
+        float h0, h1, l0, l1;
+        const int b = t.body_n[leaf];
+        f[b] = y[3 * n + b];
+        f[n + b] = y[4 * n + b];
+        f[2 * n + b] = y[5 * n + b];
+        f2_unpack(hx, h0, h1);
+        f2_unpack(lx, l0, l1);
+        f[3 * n + b] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
+        f2_unpack(hy, h0, h1);
+        f2_unpack(ly, l0, l1);
+        f[4 * n + b] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
+        f2_unpack(hz, h0, h1);
+        f2_unpack(lz, l0, l1);
+        f[5 * n + b] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
+    }
+    if (lane == 0) {
+        atomicAdd(&t.counters[0], tests);
+        atomicAdd(&t.counters[1], inter * 32ull);
+    }
+}
+
 }  // namespace
 
 nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f) {
@@ -169,6 +360,17 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
     if (e->params.learned) return learned_walk(e, y, f);
     const float eps2 = (float)(e->params.softening * e->params.softening);
     const bool clamp = !(e->params.softening > 0.0);
+    if (e->tune_get("bh.walk", 1) == 1 && n >= 32) {
+        const size_t smem = sizeof(GroupSmem);
+        auto kern = clamp ? bh_group_walk_kernel<true> : bh_group_walk_kernel<false>;
+        NBG_CUDA(e, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem));
+        const int warps = (n + 31) / 32;
+        kern<<<(warps + kGWWarps - 1) / kGWWarps, kGWThreads, smem, e->stream>>>(y, f, n, eps2, *t,
+                                                                                e->d_err);
+        NBG_LAUNCHED(e, "bh_group_walk_kernel");
+        return NBG_OK;
+    }
     // warps past n still walk (their lanes mirror the last body) so that
     // every warp is full; n is a power of two, so only n < 32 has such lanes
     const int threads = ((n + 31) / 32) * 32;

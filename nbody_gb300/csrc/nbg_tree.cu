@@ -60,29 +60,36 @@ radix_hist_kernel(const uint64_t* __restrict__ keys, int n, int shift, unsigned*
     for (int d = threadIdx.x; d < kDigits; d += kSortThreads) hist[d * gridDim.x + blockIdx.x] = h[d];
 }
 
-// Exclusive scan of hist in (digit, block) order, in place; one CTA.
-__global__ void __launch_bounds__(1024) radix_scan_kernel(unsigned* __restrict__ hist, int count) {
-    __shared__ unsigned partial[1024];
-    const int per = (count + 1023) / 1024;
-    const int b0 = threadIdx.x * per;
-    unsigned s = 0;
-    for (int k = 0; k < per; ++k)
-        if (b0 + k < count) s += hist[b0 + k];
-    partial[threadIdx.x] = s;
+// Per digit (one CTA each): exclusive scan of hist[d][0 .. nblocks) in
+// place, and the digit's total in totals[d].  The scatter kernel adds the
+// prefix of the totals (the digit base) itself.
+__global__ void __launch_bounds__(512)
+radix_digit_scan_kernel(unsigned* __restrict__ hist, int nblocks, unsigned* __restrict__ totals) {
+    __shared__ unsigned warp_tot[16];
+    __shared__ unsigned carry;
+    const int d = blockIdx.x;
+    unsigned* h = hist + (size_t)d * nblocks;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {  // Hillis-Steele inclusive scan
-        unsigned v = threadIdx.x >= off ? partial[threadIdx.x - off] : 0u;
+    for (int b0 = 0; b0 < nblocks; b0 += 512) {
+        const int b = b0 + threadIdx.x;
+        const unsigned v = b < nblocks ? h[b] : 0u;
+        unsigned incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) warp_tot[warp] = incl;
         __syncthreads();
-        partial[threadIdx.x] += v;
+        unsigned base = carry;
+        for (int w = 0; w < warp; ++w) base += warp_tot[w];
+        if (b < nblocks) h[b] = base + incl - v;
+        __syncthreads();
+        if (threadIdx.x == 511) carry = base + incl;
         __syncthreads();
     }
-    unsigned run = threadIdx.x ? partial[threadIdx.x - 1] : 0u;
-    for (int k = 0; k < per; ++k)
-        if (b0 + k < count) {
-            unsigned v = hist[b0 + k];
-            hist[b0 + k] = run;
-            run += v;
-        }
+    if (threadIdx.x == 0) totals[d] = carry;
 }
 
 // Stable scatter.  Each warp owns 256 consecutive keys of the tile and walks
@@ -92,9 +99,24 @@ __global__ void __launch_bounds__(1024) radix_scan_kernel(unsigned* __restrict__
 __global__ void __launch_bounds__(kSortThreads)
 radix_scatter_kernel(const uint64_t* __restrict__ kin, const int* __restrict__ vin,
                      uint64_t* __restrict__ kout, int* __restrict__ vout, int n, int shift,
-                     const unsigned* __restrict__ offsets) {
+                     const unsigned* __restrict__ offsets, const unsigned* __restrict__ totals) {
     constexpr int kWarpsS = kSortThreads / 32;
     __shared__ unsigned cnt[kWarpsS][kDigits];
+    __shared__ unsigned digit_base[kDigits];
+    // exclusive prefix of the digit totals (Hillis-Steele, one digit per thread)
+    static_assert(kDigits == kSortThreads, "one digit per thread");
+    {
+        const unsigned own = totals[threadIdx.x];
+        digit_base[threadIdx.x] = own;
+        __syncthreads();
+        for (int o = 1; o < kDigits; o <<= 1) {
+            const unsigned v = threadIdx.x >= (unsigned)o ? digit_base[threadIdx.x - o] : 0u;
+            __syncthreads();
+            digit_base[threadIdx.x] += v;
+            __syncthreads();
+        }
+        digit_base[threadIdx.x] -= own;  // inclusive -> exclusive
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int d = lane; d < kDigits; d += 32) cnt[warp][d] = 0;
     __syncwarp();
@@ -124,7 +146,7 @@ radix_scatter_kernel(const uint64_t* __restrict__ kin, const int* __restrict__ v
     __syncthreads();
     // per-digit prefix over warps (warp order = key order inside the tile)
     for (int d = threadIdx.x; d < kDigits; d += kSortThreads) {
-        unsigned run = offsets[d * gridDim.x + blockIdx.x];
+        unsigned run = digit_base[d] + offsets[d * gridDim.x + blockIdx.x];
         for (int w = 0; w < kWarpsS; ++w) {
             const unsigned c = cnt[w][d];
             cnt[w][d] = run;
@@ -351,6 +373,7 @@ nbg_status tree_alloc(nbg_engine* e) {
     NBG_TRY(alloc(e, &t->flag, n));
     NBG_TRY(alloc(e, &t->tile_count, 2 * ntiles));
     NBG_TRY(alloc(e, &t->hist, kDigits * nblocks));
+    NBG_TRY(alloc(e, &t->totals, kDigits));
     NBG_TRY(alloc(e, &t->com, 3 * sz));
     NBG_TRY(alloc(e, &t->mass, sz));
     NBG_TRY(alloc(e, &t->bmin, 3 * sz));
@@ -377,10 +400,10 @@ nbg_status radix_sort(nbg_engine* e, TreeState* t, int n) {
         const int src = pass & 1, dst = src ^ 1;
         radix_hist_kernel<<<nblocks, kSortThreads, 0, e->stream>>>(t->keys[src], n, shift, t->hist);
         NBG_LAUNCHED(e, "radix_hist_kernel");
-        radix_scan_kernel<<<1, 1024, 0, e->stream>>>(t->hist, kDigits * nblocks);
-        NBG_LAUNCHED(e, "radix_scan_kernel");
+        radix_digit_scan_kernel<<<kDigits, 512, 0, e->stream>>>(t->hist, nblocks, t->totals);
+        NBG_LAUNCHED(e, "radix_digit_scan_kernel");
         radix_scatter_kernel<<<nblocks, kSortThreads, 0, e->stream>>>(
-            t->keys[src], t->vals[src], t->keys[dst], t->vals[dst], n, shift, t->hist);
+            t->keys[src], t->vals[src], t->keys[dst], t->vals[dst], n, shift, t->hist, t->totals);
         NBG_LAUNCHED(e, "radix_scatter_kernel");
     }
     return NBG_OK;  // 8 passes: the result is back in keys[0] / vals[0]
@@ -403,7 +426,7 @@ void tree_destroy(nbg_engine* e) {
     TreeState* t = e->tree;
     if (t == nullptr) return;
     void* ptrs[] = {t->keys[0], t->keys[1], t->vals[0], t->vals[1], t->lists[0], t->lists[1],
-                    t->lists[2], t->spare[0], t->spare[1], t->flag, t->tile_count, t->hist,
+                    t->lists[2], t->spare[0], t->spare[1], t->flag, t->tile_count, t->hist, t->totals,
                     t->com, t->mass, t->bmin, t->bmax, t->crit2, t->body_n, t->node4,
                     t->nodem, t->feat, t->counters};
     for (void* p : ptrs) cudaFree(p);

@@ -25,6 +25,7 @@ struct TreeState {
     unsigned char* flag = nullptr;           // [n] 1 = goes to the left child
     int* tile_count = nullptr;               // [2][n / kPartTile + 1]
     unsigned* hist = nullptr;                // radix per-block digit counts
+    unsigned* totals = nullptr;              // radix per-digit totals
 
     // heap arrays, FP64 SoA (the reference's node fields)
     double* com = nullptr;    // [3][size] mass centre

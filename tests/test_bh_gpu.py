@@ -83,16 +83,19 @@ def _rel(a, a_ref):
     return np.linalg.norm(a - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
 
 
+@pytest.mark.parametrize("walk", [0, 1])
 @pytest.mark.parametrize("lam", [2.0, 1.0 / 0.9])
-def test_bh_mixed_error_vs_direct(make_engine, oracle, lam):
-    """The warp-coherent FP32 walk is at least as accurate as the reference's
-    own per-body FP64 walk (simple_bh heap_stackless) at the same ratio, both
+def test_bh_mixed_error_vs_direct(make_engine, oracle, lam, walk):
+    """Both FP32 walks (0: warp-coherent stackless, 1: group walk with
+    interaction lists) are at least as accurate as the reference's own
+    per-body FP64 walk (simple_bh heap_stackless) at the same ratio, all
     judged against the FP64 direct sum."""
     n = 16384
     d = NBodyData.plummer(n, seed=4)
     y = d.to_state()
     e = make_engine(algo="bh", precision="mixed", softening=0.0,
                     distance_to_node_radius_ratio=lam)
+    e.tune_set("bh.walk", walk)
     assert e.init(d)
     f = _f(e, y)
     rows = np.random.default_rng(9).choice(n, size=512, replace=False)
@@ -102,10 +105,34 @@ def test_bh_mixed_error_vs_direct(make_engine, oracle, lam):
     a_bh = f_bh[3 * n:].reshape(3, n).T[rows]
     rel, rel_ref = _rel(a, a_ref), _rel(a_bh, a_ref)
     visits, inter = e.bh_counters()
-    print(f"\nBH mixed lambda={lam:.3f}: p50 {np.median(rel):.2e} p99 {np.quantile(rel, 0.99):.2e}"
+    print(f"\nBH mixed walk={walk} lambda={lam:.3f}: p50 {np.median(rel):.2e} p99 {np.quantile(rel, 0.99):.2e}"
           f" (reference walk p50 {np.median(rel_ref):.2e} p99 {np.quantile(rel_ref, 0.99):.2e});"
           f" interactions/body {inter / n:.0f}, visits/warp {visits / (n / 32):.0f}")
     assert np.array_equal(f[:3 * n], y[3 * n:])
+    assert np.quantile(rel, 0.99) <= np.quantile(rel_ref, 0.99)
+    assert np.median(rel) <= np.median(rel_ref)
+
+
+@pytest.mark.parametrize("n", [32, 64, 1024])
+def test_bh_group_walk_small(make_engine, oracle, n):
+    """Group walk on one or a few warps.  One warp (n = 32) opens the whole
+    tree down to its leaves and is a direct sum; larger systems are at least
+    as accurate as the reference's per-body walk at the same ratio."""
+    d = NBodyData.plummer(n, seed=n)
+    y = d.to_state()
+    e = make_engine(algo="bh", precision="mixed", softening=0.0,
+                    distance_to_node_radius_ratio=2.0)
+    assert e.init(d)
+    f = _f(e, y)
+    a_ref = oracle.accel_rows(y, d.mass, 0.0, rows=np.arange(n))
+    a = f[3 * n:].reshape(3, n).T
+    rel = _rel(a, a_ref)
+    assert np.array_equal(f[:3 * n], y[3 * n:])
+    if n == 32:
+        assert np.max(rel) < 1e-5
+        return
+    f_bh = oracle.fcompute_bh(y, d.mass, 2.0, layout=2, traverse=0)[0]
+    rel_ref = _rel(f_bh[3 * n:].reshape(3, n).T, a_ref)
     assert np.quantile(rel, 0.99) <= np.quantile(rel_ref, 0.99)
     assert np.median(rel) <= np.median(rel_ref)
 
