@@ -214,15 +214,22 @@ def read_traffic():
     return None
 
 
-def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 5):
-    """Barnes-Hut fcompute (tree rebuilt every call) at opening ratio lam."""
+def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 5, walk: int = 1,
+             weights=None):
+    """Barnes-Hut fcompute (tree rebuilt every call) at opening ratio lam.
+    walk 1 = group walk with interaction lists, 0 = warp-coherent stackless."""
     from nbody_gb300 import _lib
     from nbody_gb300.engine import create_engine
     e = create_engine({"engine": "gb300", "algo": "bh", "precision": "mixed",
                        "softening": SOFTENING, "distance_to_node_radius_ratio": lam,
                        "learned": learned, "tree_layout": "heap_stackless"})
-    if e is None or not e.init(d):
+    if e is None:
         return {"unavailable": "engine not created"}
+    e.tune_set("bh.walk", walk)
+    if not e.init(d):
+        return {"unavailable": "engine init failed"}
+    if weights is not None:
+        e.learn_set_weights(weights)
     f = e.create_buffer(8 * 6 * n_bh)
     for _ in range(2):
         e.fcompute(0.0, e.get_y(), f)
@@ -243,12 +250,41 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
     rel = np.linalg.norm(a - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
     e.close()
     ms = (tb / max(nb, 1) + tw / max(nw, 1))
-    return {"lambda": lam, "theta": 1.0 / lam, "bodies_per_s": n_bh / (ms * 1e-3),
+    # node records read by the walk (20 B each: com.xyz + crit^2, mass), per
+    # warp test, plus the body rows (16 B in, 24 B out)
+    walk_bytes = visits / calls * 20.0 + n_bh * 40.0
+    return {"lambda": lam, "theta": 1.0 / lam, "walk": walk, "learned": learned,
+            "bodies_per_s": n_bh / (ms * 1e-3),
+            "walk_node_gbs": walk_bytes / (tw / max(nw, 1) * 1e-3) / 1e9,
             "ms_per_fcompute": ms, "wall_ms_per_fcompute": wall * 1e3,
             "build_ms": tb / max(nb, 1), "walk_ms": tw / max(nw, 1),
             "p50": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99)),
             "interactions_per_body": inter / calls / n_bh,
             "warp_node_visits_per_warp": visits / calls / (n_bh / 32)}
+
+
+def train_correction(epochs: int = 8):
+    """Samples from two snapshots the timed one is not (Plummer and uniform
+    cube, N = 2^16), trained on the GPU; returns the weights and the fit."""
+    from nbody_gb300.data import NBodyData
+    from nbody_gb300.engine import create_engine
+    e = create_engine({"engine": "gb300", "algo": "bh", "precision": "mixed",
+                       "softening": SOFTENING, "distance_to_node_radius_ratio": 1.0 / 0.9,
+                       "learned_tight_ratio": 2.0})
+    t0 = time.perf_counter()
+    total = 0
+    for i, d in enumerate((NBodyData.plummer(1 << 16, seed=41),
+                           NBodyData.uniform_cube(1 << 16, side=2.0, seed=42))):
+        e.init(d)
+        total += e.learn_generate(500000, seed=50 + i)
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    tr, va = e.learn_train(epochs, batch=8192, lr=3e-3, seed=5)
+    train_s = time.perf_counter() - t0
+    w = e.learn_get_weights()
+    e.close()
+    return w, {"samples": total, "epochs": epochs, "train_mse": tr, "val_mse": va,
+               "generate_s": gen_s, "train_s": train_s}
 
 
 def run_bh_suite(rank: int, n_bh: int = 1 << 20):
@@ -264,6 +300,14 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20):
            "error_judge": "FP64 direct sum (oracle) on 4096 sampled bodies"}
     res["plain_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d)
     res["plain_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d)
+    res["coherent_walk_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, walk=0)
+    w, fit = train_correction()
+    res["learned_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=w)
+    res["learned_theta_0.9"]["training"] = fit
+    p05, l09 = res["plain_theta_0.5"], res["learned_theta_0.9"]
+    res["learned_0.9_vs_plain_0.5"] = {
+        "bodies_per_s_ratio": l09["bodies_per_s"] / p05["bodies_per_s"],
+        "p99_ratio": l09["p99"] / p05["p99"]}
     return res
 
 

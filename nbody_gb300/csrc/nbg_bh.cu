@@ -19,6 +19,11 @@
 //    so every load is a warp-wide broadcast and the walk never diverges.
 //    Each lane's accepted set refines its own per-body set, so the result is
 //    at least as accurate as the per-body walk at the same opening ratio.
+//    This walk is the one the learned correction extends (bh.walk = 0).
+//  * group walk (precision mixed, the default, bh.walk = 1): a warp tests 32
+//    nodes at a time against the bounding box of its 32 bodies and evaluates
+//    the accepted nodes from an interaction list in shared memory with packed
+//    FP32x2 pair math (details at bh_group_walk_kernel).
 #include "nbg_ptx.cuh"
 #include "nbg_tree.cuh"
 
