@@ -220,7 +220,9 @@ nbg_status nbg_tree_leaves(nbg_engine* e, int* body_of_leaf);
 uint64_t nbg_launch_count(const nbg_engine* e);
 
 /* Tuning knobs (set by the autotuner or by hand; no reference counterpart).
- * Keys: "direct.pairs_per_lane" (2 or 4 packed i-pairs per lane),
+ * Keys: "direct.symmetric" (1: each unordered pair evaluated once and
+ *       applied to both bodies, the default; 0: one-sided kernel),
+ *       "direct.pairs_per_lane" (2 or 4 packed i-pairs per lane, one-sided),
  *       "direct.unroll" (2, 4 or 8: j-loop unroll),
  *       "direct.blocks_per_sm" (CTAs per SM of the persistent direct grid),
  *       "bh.walk" (1: group walk with interaction lists, 0: warp-coherent

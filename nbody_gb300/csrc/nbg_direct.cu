@@ -1,6 +1,6 @@
 // nbg_direct.cu -- direct O(N^2) gravity: f = [v ; a(y)].
 //
-// Two kernels share the engine entry point:
+// Three kernels share the engine entry point:
 //
 //  * FP64 (parity) -- one thread per body, j-tiles of double4 in shared
 //    memory, the reference 'simple' arithmetic in the reference order
@@ -21,6 +21,10 @@
 //    with one atomicAdd per component.  Pair term:
 //        a_i += m_j (r_j - r_i) / (|r_j - r_i|^2 + eps^2)^{3/2}
 //    with r^2 clamped to >= 1e-8 when eps = 0 (the reference clamp).
+//
+//  * mixed, symmetric (the default, tuning key direct.symmetric = 1) -- the
+//    same arithmetic with every unordered pair evaluated once and applied to
+//    both bodies (details at direct_sym_kernel).
 #include <mutex>
 
 #include "nbg_internal.cuh"
@@ -313,6 +317,350 @@ MixedKernel pick_mixed(int G, int unr) {
     return direct_mixed_kernel<CLAMP, 2, 4>;
 }
 
+// ---------------------------------------------------------------------------
+// symmetric mixed kernel: every unordered pair evaluated once
+// ---------------------------------------------------------------------------
+// Bodies are split into ranges of kSymRange.  A CTA holds one range in
+// registers (the A bodies: 8 per lane, as 4 packed FP32x2 pairs) and streams
+// 128-body B tiles through the same TMA ring as above.  Unit (R, t) pairs
+// range R with tile t for t >= the first tile of R:
+//   * t inside R: one-sided, all ordered pairs, A side only (the self pair
+//     contributes d = 0);
+//   * t after R: symmetric.  Each pair adds m_B d / r^3 to A and
+//     -m_A d / r^3 to B (Newton's third law), so tiles before R are covered
+//     by the units of their own ranges.
+// Symmetric chunks of 32 B bodies rotate through the warp: at step k lane l
+// meets B body (l + k) mod 32 with its 8 A bodies, and the B accumulator
+// follows its body one lane down per step (a shuffle), so after 32 steps lane
+// l holds the complete warp sum for B body l and adds it to f with FP64
+// reductions.  Per pair this costs 16 FP32 operations and one reciprocal
+// square root for two interactions, against 12 and one per interaction in
+// the one-sided kernel.
+constexpr int kSymWarps = 4;
+constexpr int kSymThreads = kSymWarps * 32;
+constexpr int kSymG = 4;
+constexpr int kSymRange = kSymThreads * 2 * kSymG;  // 1024 A bodies per range
+constexpr int kSymT = 128;                            // B bodies per tile
+constexpr int kSymTilesPerRange = kSymRange / kSymT;  // 8
+constexpr int kSymStages = 4;
+constexpr uint32_t kSymTileBytes = kSymT * 32;  // (x x y y | z z m m) FP32 per body
+
+struct SymArgs {
+    const float4* bodies;  // [2 n_pad], tile-split layout
+    double* acc;           // a-part of f: [3][n]
+    int n;
+    int n_jt;              // tiles = n_pad / kSymT
+    int n_ranges;          // n_pad / kSymRange
+    long long units;
+    float eps2;
+    unsigned* err;
+};
+
+// Tile-split layout: tile t holds [(x x y y) x 128 | (z z m m) x 128], so a
+// lane's two LDS.128 of one body return both packed operands ready for the
+// FP32x2 arithmetic, and 32 lanes reading 32 different bodies touch 512
+// contiguous bytes per load.
+__device__ __forceinline__ size_t sym_xy(int i) { return (size_t)(i >> 7) * 256 + (i & 127); }
+
+__global__ void pack_sym_kernel(const double* __restrict__ y, const double* __restrict__ mass,
+                                float4* __restrict__ out, double* __restrict__ f, int n,
+                                int n_pad) {
+    int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += stride) {
+        float4 xy = make_float4(0.f, 0.f, 0.f, 0.f), zm = xy;
+        if (i < n) {
+            const float x = (float)y[i], yy = (float)y[n + i], z = (float)y[2 * n + i];
+            const float m = (float)mass[i];
+            xy = make_float4(x, x, yy, yy);
+            zm = make_float4(z, z, m, m);
+            f[i] = y[3 * n + i];
+            f[n + i] = y[4 * n + i];
+            f[2 * n + i] = y[5 * n + i];
+            f[3 * n + i] = 0.0;
+            f[4 * n + i] = 0.0;
+            f[5 * n + i] = 0.0;
+        }
+        out[sym_xy(i)] = xy;
+        out[sym_xy(i) + kSymT] = zm;
+    }
+}
+
+// First unit of range R: sum over R' < R of (n_jt - 8 R').
+__device__ __forceinline__ long long sym_range_start(long long R, long long n_jt) {
+    return R * n_jt - (long long)kSymTilesPerRange * (R * (R - 1) / 2);
+}
+
+struct SymCursor {
+    int R, t;
+    __device__ void locate(long long u, int n_jt, int n_ranges) {
+        int lo = 0, hi = n_ranges - 1;  // largest R with start(R) <= u
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (sym_range_start(mid, n_jt) <= u) lo = mid;
+            else hi = mid - 1;
+        }
+        R = lo;
+        t = (int)(u - sym_range_start(lo, n_jt)) + kSymTilesPerRange * lo;
+    }
+    __device__ void next(int n_jt) {
+        if (++t == n_jt) {
+            ++R;
+            t = kSymTilesPerRange * R;
+        }
+    }
+};
+
+template <bool CLAMP>
+__device__ __forceinline__ void sym_pair(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f2_t xi, f2_t yi,
+                                         f2_t zi, f2_t mi, f2_t eps2, f2_t& ax, f2_t& ay,
+                                         f2_t& az, f2_t& bx, f2_t& by, f2_t& bz) {
+    const f2_t dx = f2_sub(xj, xi);
+    const f2_t dy = f2_sub(yj, yi);
+    const f2_t dz = f2_sub(zj, zi);
+    f2_t r2 = f2_fma(dz, dz, eps2);
+    r2 = f2_fma(dy, dy, r2);
+    r2 = f2_fma(dx, dx, r2);
+    float r2a, r2b;
+    f2_unpack(r2, r2a, r2b);
+    if (CLAMP) {
+        r2a = fmaxf(r2a, 1e-8f);
+        r2b = fmaxf(r2b, 1e-8f);
+    }
+    const f2_t inv = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
+    const f2_t inv3 = f2_mul(f2_mul(inv, inv), inv);
+    const f2_t sa = f2_mul(mj, inv3);
+    const f2_t sb = f2_mul(mi, inv3);
+    ax = f2_fma(dx, sa, ax);
+    ay = f2_fma(dy, sa, ay);
+    az = f2_fma(dz, sa, az);
+    bx = f2_fma(dx, sb, bx);
+    by = f2_fma(dy, sb, by);
+    bz = f2_fma(dz, sb, bz);
+}
+
+__device__ __forceinline__ void sym_issue(float4* tiles, uint64_t* full, int s, int t,
+                                          const float4* bodies) {
+    mbar_arrive_expect_tx(&full[s], kSymTileBytes);
+    bulk_g2s(tiles + s * 2 * kSymT, bodies + (size_t)t * 2 * kSymT, kSymTileBytes, &full[s]);
+}
+
+template <bool CLAMP>
+__global__ void __launch_bounds__(kSymThreads, 4)
+direct_sym_kernel(SymArgs a) {
+    constexpr int G = kSymG;
+    constexpr int kSlots = 6 * G;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float4* tiles = reinterpret_cast<float4*>(smem_raw);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + kSymStages * kSymTileBytes);
+    uint64_t* empty = full + kSymStages;
+    f2_t* acc_sm = reinterpret_cast<f2_t*>(smem_raw + kSymStages * kSymTileBytes +
+                                           2 * kSymStages * sizeof(uint64_t));
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long per = a.units / gridDim.x;
+    const long long rem = a.units % gridDim.x;
+    const long long u0 = blockIdx.x * per + min((long long)blockIdx.x, rem);
+    const long long cnt = per + ((long long)blockIdx.x < rem ? 1 : 0);
+    const bool producer = threadIdx.x == 0;
+    auto acc_at = [&](int q) -> f2_t& { return acc_sm[q * kSymThreads + threadIdx.x]; };
+
+    if (producer) {
+        for (int s = 0; s < kSymStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kSymWarps);
+        }
+        mbar_fence_init();
+    }
+    __syncthreads();
+    SymCursor cons, prod;
+    cons.locate(u0, a.n_jt, a.n_ranges);
+    prod = cons;
+    if (producer) {
+        for (long long k = 0; k < kSymStages && k < cnt; ++k) {
+            sym_issue(tiles, full, (int)k, prod.t, a.bodies);
+            prod.next(a.n_jt);
+        }
+    }
+
+    const f2_t eps2 = f2_pack(a.eps2, a.eps2);
+    const f2_t zero = f2_pack(0.f, 0.f);
+    f2_t xi[G], yi[G], zi[G], mi[G];
+    int cur_R = -1;
+    bool ok = true;
+    const uint32_t tiles_addr = smem_addr(tiles);
+
+    auto flush = [&](int R) {
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            float h0, h1, l0, l1;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                f2_unpack(acc_at(2 * (3 * g + c)), h0, h1);
+                f2_unpack(acc_at(2 * (3 * g + c) + 1), l0, l1);
+                const int i0 = R * kSymRange + (2 * g) * kSymThreads + warp * 32 + lane;
+                const int i1 = i0 + kSymThreads;
+                if (i0 < a.n) atomicAdd(a.acc + (size_t)c * a.n + i0, (double)h0 + (double)l0);
+                if (i1 < a.n) atomicAdd(a.acc + (size_t)c * a.n + i1, (double)h1 + (double)l1);
+            }
+        }
+    };
+
+    for (long long k = 0; k < cnt; ++k) {
+        if (producer && k >= 1 && k - 1 + kSymStages < cnt) {
+            const int sp = (int)((k - 1) % kSymStages);
+            const uint32_t par = (uint32_t)(((k - 1) / kSymStages) & 1);
+            if (!mbar_wait(&empty[sp], par, a.err)) {
+                ok = false;
+                break;
+            }
+            sym_issue(tiles, full, sp, prod.t, a.bodies);
+            prod.next(a.n_jt);
+        }
+        if (cons.R != cur_R) {
+            if (cur_R >= 0) flush(cur_R);
+            cur_R = cons.R;
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                const int i0 = cur_R * kSymRange + (2 * g) * kSymThreads + warp * 32 + lane;
+                const float4 p0 = __ldg(&a.bodies[sym_xy(i0)]);
+                const float4 q0 = __ldg(&a.bodies[sym_xy(i0) + kSymT]);
+                const float4 p1 = __ldg(&a.bodies[sym_xy(i0 + kSymThreads)]);
+                const float4 q1 = __ldg(&a.bodies[sym_xy(i0 + kSymThreads) + kSymT]);
+                xi[g] = f2_pack(p0.x, p1.x);
+                yi[g] = f2_pack(p0.z, p1.z);
+                zi[g] = f2_pack(q0.x, q1.x);
+                mi[g] = f2_pack(q0.z, q1.z);
+            }
+#pragma unroll
+            for (int q = 0; q < kSlots; ++q) acc_at(q) = zero;
+        }
+        const int s = (int)(k % kSymStages);
+        if (!mbar_wait(&full[s], (uint32_t)((k / kSymStages) & 1), a.err)) {
+            ok = false;
+            break;
+        }
+        const uint32_t tbase = tiles_addr + (uint32_t)s * kSymTileBytes;
+        f2_t ax[G], ay[G], az[G];
+#pragma unroll
+        for (int g = 0; g < G; ++g) ax[g] = ay[g] = az[g] = zero;
+        if (cons.t < kSymTilesPerRange * (cons.R + 1)) {
+            // own range: one-sided, broadcast loads
+#pragma unroll 4
+            for (int j = 0; j < kSymT; ++j) {
+                const float4 p = lds128(tbase + 16u * j);
+                const float4 q = lds128(tbase + 16u * (j + kSymT));
+                const f2_t xj = f2_pack(p.x, p.y);
+                const f2_t yj = f2_pack(p.z, p.w);
+                const f2_t zj = f2_pack(q.x, q.y);
+                const f2_t mj = f2_pack(q.z, q.w);
+#pragma unroll
+                for (int g = 0; g < G; ++g)
+                    pair2<CLAMP>(xj, yj, zj, mj, xi[g], yi[g], zi[g], eps2, ax[g], ay[g], az[g]);
+            }
+        } else {
+#pragma unroll 1
+            for (int c = 0; c < kSymT / 32; ++c) {
+                const uint32_t cbase = tbase + (uint32_t)c * 512u;
+                float bx = 0.f, by = 0.f, bz = 0.f;
+#pragma unroll 2
+                for (int r = 0; r < 32; ++r) {
+                    const uint32_t off = cbase + ((uint32_t)((lane + r) & 31) << 4);
+                    const float4 p = lds128(off);
+                    const float4 q = lds128(off + 16u * kSymT);
+                    const f2_t xj = f2_pack(p.x, p.y);
+                    const f2_t yj = f2_pack(p.z, p.w);
+                    const f2_t zj = f2_pack(q.x, q.y);
+                    const f2_t mj = f2_pack(q.z, q.w);
+                    f2_t px = zero, py = zero, pz = zero;
+#pragma unroll
+                    for (int g = 0; g < G; ++g)
+                        sym_pair<CLAMP>(xj, yj, zj, mj, xi[g], yi[g], zi[g], mi[g], eps2, ax[g],
+                                        ay[g], az[g], px, py, pz);
+                    float l, h;
+                    f2_unpack(px, l, h);
+                    bx += l + h;
+                    f2_unpack(py, l, h);
+                    by += l + h;
+                    f2_unpack(pz, l, h);
+                    bz += l + h;
+                    // the accumulator of B body (lane + r) moves to lane - 1,
+                    // which meets that body at step r + 1
+                    const int src = (lane + 1) & 31;
+                    bx = __shfl_sync(0xffffffffu, bx, src);
+                    by = __shfl_sync(0xffffffffu, by, src);
+                    bz = __shfl_sync(0xffffffffu, bz, src);
+                }
+                // after 32 steps and shifts lane l holds the sum for B body l
+                const int jb = cons.t * kSymT + c * 32 + lane;
+                if (jb < a.n) {
+                    atomicAdd(a.acc + jb, -(double)bx);
+                    atomicAdd(a.acc + (size_t)a.n + jb, -(double)by);
+                    atomicAdd(a.acc + 2 * (size_t)a.n + jb, -(double)bz);
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            f2_two_sum(acc_at(2 * (3 * g + 0)), acc_at(2 * (3 * g + 0) + 1), ax[g]);
+            f2_two_sum(acc_at(2 * (3 * g + 1)), acc_at(2 * (3 * g + 1) + 1), ay[g]);
+            f2_two_sum(acc_at(2 * (3 * g + 2)), acc_at(2 * (3 * g + 2) + 1), az[g]);
+        }
+        cons.next(a.n_jt);
+    }
+    if (ok && cur_R >= 0) flush(cur_R);
+}
+
+size_t sym_smem_bytes() {
+    return (size_t)kSymStages * kSymTileBytes + 2 * kSymStages * sizeof(uint64_t) +
+           6 * kSymG * kSymThreads * sizeof(f2_t);
+}
+
+nbg_status direct_sym_launch(nbg_engine* e, const double* y, double* f) {
+    const int n = (int)e->count;
+    const int n_ranges = (n + kSymRange - 1) / kSymRange;
+    const int n_pad = n_ranges * kSymRange;
+    const size_t need = 2 * (size_t)n_pad * sizeof(float4);
+    if (e->xyzm_cap < need) {
+        cudaFree(e->d_xyzm);
+        e->d_xyzm = nullptr;
+        e->xyzm_cap = 0;
+        NBG_CUDA(e, cudaMalloc(&e->d_xyzm, need));
+        e->xyzm_cap = need;
+    }
+    float4* bodies = reinterpret_cast<float4*>(e->d_xyzm);
+    pack_sym_kernel<<<grid_for(n_pad, 256, (unsigned)e->sm_count * 8u), 256, 0, e->stream>>>(
+        y, e->d_mass, bodies, f, n, n_pad);
+    NBG_LAUNCHED(e, "pack_sym_kernel");
+    const bool clamp = !(e->params.softening > 0.0);
+    auto kern = clamp ? direct_sym_kernel<true> : direct_sym_kernel<false>;
+    const size_t smem = sym_smem_bytes();
+    NBG_CUDA(e, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+    int occ = 0;
+    NBG_CUDA(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kSymThreads, smem));
+    if (occ < 1) occ = 1;
+    const int64_t bps = e->tune_get("direct.blocks_per_sm", 0);
+    if (bps > 0 && bps < occ) occ = (int)bps;
+    SymArgs a;
+    a.bodies = bodies;
+    a.acc = f + 3 * (size_t)n;
+    a.n = n;
+    a.n_jt = n_pad / kSymT;
+    a.n_ranges = n_ranges;
+    a.units = (long long)n_ranges * a.n_jt -
+              (long long)kSymTilesPerRange * ((long long)n_ranges * (n_ranges - 1) / 2);
+    a.eps2 = (float)(e->params.softening * e->params.softening);
+    a.err = e->d_err;
+    long long grid = (long long)e->sm_count * occ;
+    if (grid > a.units) grid = a.units;
+    ProfScope ps(e, NBG_K_DIRECT);
+    kern<<<(unsigned)grid, kSymThreads, smem, e->stream>>>(a);
+    NBG_LAUNCHED(e, "direct_sym_kernel");
+    return NBG_OK;
+}
+
 }  // namespace
 
 nbg_status direct_fcompute(nbg_engine* e, const double* y, double* f) {
@@ -326,6 +674,7 @@ nbg_status direct_fcompute(nbg_engine* e, const double* y, double* f) {
     }
 
     // ---- mixed precision ----
+    if (e->tune_get("direct.symmetric", 1) != 0) return direct_sym_launch(e, y, f);
     const int n_jt = (n + kT - 1) / kT;
     const int n_pad = n_jt * kT;
     const size_t need = (size_t)n_pad * sizeof(Body2);

@@ -67,10 +67,14 @@ def test_config1_fp64_rk4_100_steps(make_engine, oracle):
           f"ref {abs((st_ref[6] + st_ref[7] - e0) / e0):.3e}")
 
 
-def test_mixed_plummer_force_error(make_engine, oracle):
+@pytest.mark.parametrize("sym", [0, 1])
+def test_mixed_plummer_force_error(make_engine, oracle, sym):
+    """Both mixed kernels (0: one-sided, 1: each unordered pair once) on
+    every row against the FP64 direct sum."""
     n = 16384
     d = NBodyData.plummer(n, seed=7)
     e = make_engine(precision="mixed", softening=1e-3)
+    e.tune_set("direct.symmetric", sym)
     assert e.init(d)
     y = d.to_state()
     f = _f_gpu(e, y)
@@ -78,16 +82,20 @@ def test_mixed_plummer_force_error(make_engine, oracle):
     a_ref = oracle.accel_rows(y, d.mass, 1e-3)
     rel = _rel_err(a, a_ref)
     rms, p99 = float(np.sqrt(np.mean(rel ** 2))), float(np.quantile(rel, 0.99))
-    print(f"\nmixed N={n}: rms {rms:.3e} p99 {p99:.3e} max {rel.max():.3e}")
+    print(f"\nmixed sym={sym} N={n}: rms {rms:.3e} p99 {p99:.3e} max {rel.max():.3e}")
     assert rms <= 1e-6
     assert np.array_equal(f[:3 * n], y[3 * n:])
 
 
-@pytest.mark.parametrize("n", [1, 2, 15, 63, 65, 127, 129, 513, 1000])
-@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("n", [1, 2, 15, 63, 65, 127, 129, 513, 1000, 1025, 2047, 5000])
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed-onesided"])
 def test_ragged_sizes(make_engine, oracle, n, prec):
+    """Sizes around the tile (128) and range (1024) boundaries; above 1024
+    bodies the symmetric kernel has pairs of ranges."""
     d = NBodyData.uniform_cube(n, side=10.0, seed=n)
-    e = make_engine(precision=prec)
+    e = make_engine(precision=prec.split("-")[0])
+    if prec == "mixed-onesided":
+        e.tune_set("direct.symmetric", 0)
     assert e.init(d)
     y = d.to_state()
     f = _f_gpu(e, y)
@@ -102,10 +110,12 @@ def test_ragged_sizes(make_engine, oracle, n, prec):
         assert np.all(f[3:] == 0.0)
 
 
-def test_full_size_sampled_and_momentum(make_engine, oracle):
+@pytest.mark.parametrize("sym", [0, 1])
+def test_full_size_sampled_and_momentum(make_engine, oracle, sym):
     n = 131072
     d = NBodyData.plummer(n, seed=11)
     e = make_engine(precision="mixed", softening=1e-3)
+    e.tune_set("direct.symmetric", sym)
     assert e.init(d)
     y = d.to_state()
     f = _f_gpu(e, y)
@@ -114,7 +124,7 @@ def test_full_size_sampled_and_momentum(make_engine, oracle):
     a_ref = oracle.accel_rows(y, d.mass, 1e-3, rows=rows)
     rel = _rel_err(a[rows], a_ref)
     rms = float(np.sqrt(np.mean(rel ** 2)))
-    print(f"\nmixed N={n} sampled: rms {rms:.3e} p99 {np.quantile(rel, 0.99):.3e}")
+    print(f"\nmixed sym={sym} N={n} sampled: rms {rms:.3e} p99 {np.quantile(rel, 0.99):.3e}")
     assert rms <= 1e-6
     # Newton's third law: sum m a = 0 up to rounding of the sum of |m a|
     net = np.abs((d.mass[:, None] * a).sum(axis=0))

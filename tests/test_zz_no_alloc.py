@@ -23,9 +23,11 @@ RTOL = 1e-12         # same kernel; only the order of FP64 atomic adds may diffe
 
 
 def _engine_reference(make_engine, d, eps):
-    """f from the existing entry point: a mixed-precision engine's fcompute."""
+    """f from the existing entry point: a mixed-precision engine's fcompute
+    with the one-sided kernel."""
     n = d.get_count()
     e = make_engine(precision="mixed", softening=eps)
+    e.tune_set("direct.symmetric", 0)  # the one-sided kernel the entry point runs
     assert e.init(d)
     f = e.create_buffer(8 * 6 * n)
     e.fcompute(0.0, e.get_y(), f)
