@@ -322,6 +322,7 @@ def run_ensemble_suite(steps: int = 20):
     ens = Ensemble(softening=SOFTENING, tolerance=1e-8, dt_initial=1e-3)
     ens.init(systems)
     st0 = ens.statistics()
+    tuning = ens.autotune(3)  # force-kernel tile shape and grid, timed on this state
     ens.step(1)  # warm-up (captures the graph)
     ens.synchronize()
     _, _, acc0, rej0 = ens.status()
@@ -348,7 +349,10 @@ def run_ensemble_suite(steps: int = 20):
             "ms_per_step": wall / steps * 1e3,
             "pairs_per_s": pairs / wall,
             "energy_drift_median": float(np.median(drift)),
-            "energy_drift_max": float(drift.max())}
+            "energy_drift_max": float(drift.max()),
+            "autotuner": {"best": tuning["best"],
+                          "force_ms": {json.dumps(c["keys"], sort_keys=True): round(c["ms"], 4)
+                                       for c in tuning["candidates"]}}}
 
 
 def run_gb300(args):
@@ -367,6 +371,7 @@ def run_gb300(args):
     if e is None:
         raise RuntimeError("GB300 engine could not be created")
     assert e.init(d)
+    tuning = e.autotune(3)  # kernel variant and grid, timed on this state
     s = create_solver({"solver": "rk4"})
     s.set_time_step(DT, DT)
     s.set_engine(e)
@@ -473,7 +478,8 @@ def run_gb300(args):
             "config": {"workload": WORKLOAD, "n": n, "softening": SOFTENING, "dt": DT,
                        "integrator": "rk4", "precision": "f32 pairs, two-sum tiles, f64 state",
                        "l2": "flushed between timed steps (256 MB write)",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}",
+                       "tuning": tuning["best"]},
             "roofline": {"bound": "fp32", "achieved": achieved_tflops,
                          "peak": peak_flops / 1e12, "unit": "TFLOP/s",
                          "frac": achieved_tflops / (peak_flops / 1e12),

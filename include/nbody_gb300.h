@@ -230,6 +230,14 @@ uint64_t nbg_launch_count(const nbg_engine* e);
 nbg_status nbg_tune_set(nbg_engine* e, const char* key, int64_t value);
 nbg_status nbg_tune_get(nbg_engine* e, const char* key, int64_t* value);
 
+/* Autotuner: times every candidate configuration of the engine's force path
+ * (direct: symmetric / one-sided kernel, i-pairs per lane, unroll, CTAs per
+ * SM; Barnes-Hut: walk form) on the current state, `reps` calls each after
+ * one untimed call, with CUDA events; keeps the fastest in the tuning table
+ * and writes a JSON report of all timings into report[report_len] (may be
+ * NULL).  The engine must be initialized; results in y are not touched. */
+nbg_status nbg_autotune(nbg_engine* e, int reps, char* report, size_t report_len);
+
 /* ---- allocation-free direct sum (no counterpart in the reference) ----
  * For callers that must not allocate GPU memory -- e.g. a host application
  * that hands out all device memory from its own arena, or a time-critical
@@ -290,8 +298,13 @@ nbg_status nbg_ensemble_fcompute(nbg_ensemble* s, double* f);
 /* 12 FP64 conservation sums per system (layout of nbg_statistics, softened
  * potential of the ensemble's softening). */
 nbg_status nbg_ensemble_statistics(nbg_ensemble* s, double* out);
-/* Tuning key "ensemble.pairs_per_lane" (1 or 2), read by nbg_ensemble_init. */
+/* Tuning keys "ensemble.pairs_per_lane" (1 or 2: i-tile of 256 or 512 bodies
+ * per work unit) and "ensemble.blocks_per_sm" (0 = as many as fit); a change
+ * takes effect from the next step (the step graph is captured again). */
 nbg_status nbg_ensemble_tune_set(nbg_ensemble* s, const char* key, int64_t value);
+/* Autotuner of the ensemble force kernel (tile shape and grid), timed on the
+ * current state; keeps the fastest; JSON report as nbg_autotune. */
+nbg_status nbg_ensemble_autotune(nbg_ensemble* s, int reps, char* report, size_t report_len);
 uint64_t nbg_ensemble_launch_count(const nbg_ensemble* s);
 /* Accumulated device time of the force kernel (then reset); enable/disable timing. */
 nbg_status nbg_ensemble_profile(nbg_ensemble* s, int enable, double* force_ms,

@@ -41,7 +41,8 @@ EXPORTS = [
     "nbg_ensemble_last_error", "nbg_ensemble_init", "nbg_ensemble_step",
     "nbg_ensemble_synchronize", "nbg_ensemble_status", "nbg_ensemble_get_state",
     "nbg_ensemble_fcompute", "nbg_ensemble_statistics", "nbg_ensemble_tune_set",
-    "nbg_ensemble_launch_count", "nbg_ensemble_profile",
+    "nbg_ensemble_launch_count", "nbg_ensemble_profile", "nbg_autotune",
+    "nbg_ensemble_autotune",
 ]
 
 
@@ -172,5 +173,7 @@ def load() -> C.CDLL:
     _proto(lib, "nbg_ensemble_tune_set", i32, vp, C.c_char_p, C.c_int64)
     _proto(lib, "nbg_ensemble_launch_count", u64, vp)
     _proto(lib, "nbg_ensemble_profile", i32, vp, i32, dp, C.POINTER(u64))
+    _proto(lib, "nbg_autotune", i32, vp, i32, C.c_char_p, sz)
+    _proto(lib, "nbg_ensemble_autotune", i32, vp, i32, C.c_char_p, sz)
     _lib = lib
     return lib

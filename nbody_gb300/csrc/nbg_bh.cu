@@ -157,31 +157,33 @@ bh_walk_mixed_kernel(const double* __restrict__ y, double* __restrict__ f, int n
 // ---------------------------------------------------------------------------
 // group walk: 32 nodes tested per warp step, interactions evaluated in batches
 // ---------------------------------------------------------------------------
-// A warp owns 32 consecutive leaves (a compact kd subtree).  It walks the heap
-// breadth-first-by-32: each step pops up to 32 candidate nodes from a warp
-// stack in shared memory, one per lane, and tests each against the bounding
-// box of the 32 bodies: a node is accepted when the box's nearest point is
-// outside the node's critical radius (then every body of the group accepts
-// it); leaves are always accepted (a body meets itself at distance 0, which
-// contributes nothing); other nodes are opened and their two children pushed.
-// Accepted nodes go to an interaction list, stored pairwise as
-// (x x | y y | z z | m m) records so one LDS.128 feeds FP32x2 operands, and
-// every lane evaluates the list for its own body with the direct-sum pair
-// kernel.  Each body's accepted set refines its per-body set (box distance
-// <= body distance), so the result is at least as accurate as the
-// reference's per-body walk at the same ratio.
+// A warp owns 32 consecutive leaves (a compact kd subtree).  Its stack holds
+// opened nodes; an entry c stands for the two children 2c and 2c + 1.  Each
+// step pops up to 16 entries, so each lane tests one node, against the
+// bounding box of the warp's 32 bodies: a node is accepted when the box's
+// nearest point is outside the node's critical radius (then every body of
+// the group accepts it); leaves are always accepted (a body meets itself at
+// distance 0, which contributes nothing); other nodes are opened and pushed.
+// The walk starts from entry 0, whose children are the unused heap slot 0
+// (skipped) and the root.  Accepted nodes go to an interaction list kept as
+// four float arrays (x, y, z, m): the stores of one step are consecutive,
+// and one LDS.128 of an array returns two aligned FP32x2 operand pairs.
+// When the list fills, every lane evaluates it for its own body with the
+// direct-sum pair term and folds the result into two-sum accumulators.
+// Each body's accepted set refines its per-body set (box distance <= body
+// distance), so the result is at least as accurate as the reference's
+// per-body walk at the same ratio.
 constexpr int kGWWarps = 4;
 constexpr int kGWThreads = kGWWarps * 32;
-constexpr int kGWStack = 1536;  // node indices per warp
-constexpr int kGWList = 256;    // interaction entries per warp (128 records)
-
-struct PairRec {
-    float x[2], y[2], z[2], m[2];
-};
+constexpr int kGWStack = 1024;  // entries per warp; a walk needs about 32 per tree level
+constexpr int kGWList = 256;    // interaction entries per warp
 
 struct GroupSmem {
     int stack[kGWWarps][kGWStack];
-    PairRec list[kGWWarps][kGWList / 2];
+    float lx[kGWWarps][kGWList];
+    float ly[kGWWarps][kGWList];
+    float lz[kGWWarps][kGWList];
+    float lm[kGWWarps][kGWList];
 };
 
 template <bool CLAMP>
@@ -229,55 +231,61 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
             hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
         }
     int* stack = S.stack[warp];
-    PairRec* list = S.list[warp];
-    const uint32_t list_addr = smem_addr(list);
+    float* lx = S.lx[warp];
+    float* ly = S.ly[warp];
+    float* lz = S.lz[warp];
+    float* lm = S.lm[warp];
+    const uint32_t ax_addr = smem_addr(lx), ay_addr = smem_addr(ly);
+    const uint32_t az_addr = smem_addr(lz), am_addr = smem_addr(lm);
     const f2_t eps2 = f2_pack(eps2v, eps2v);
     const f2_t zero = f2_pack(0.f, 0.f);
     const f2_t xi = f2_pack(me.x, me.x), yi = f2_pack(me.y, me.y), zi = f2_pack(me.z, me.z);
-    f2_t hx = zero, hy = zero, hz = zero, lx = zero, ly = zero, lz = zero;
+    f2_t hx = zero, hy = zero, hz = zero, qx = zero, qy = zero, qz = zero;
     const unsigned lt = (1u << lane) - 1u;
     unsigned long long tests = 0, inter = 0;
-    if (lane == 0) stack[0] = 1;
+    if (lane == 0) stack[0] = 0;
     __syncwarp();
     int sp = 1, lc = 0;
     bool overflow = false;
 
     auto evaluate = [&]() {
-        if (lc & 1) {  // pad to whole records with a massless entry
-            if (lane == 0) {
-                PairRec& r = list[lc >> 1];
-                r.x[1] = 0.f;
-                r.y[1] = 0.f;
-                r.z[1] = 0.f;
-                r.m[1] = 0.f;
-            }
-            __syncwarp();
+        // pad to a whole quad with massless entries
+        const int pad = (4 - (lc & 3)) & 3;
+        if (lane < pad) {
+            lx[lc + lane] = 0.f;
+            ly[lc + lane] = 0.f;
+            lz[lc + lane] = 0.f;
+            lm[lc + lane] = 0.f;
         }
+        __syncwarp();
         f2_t ax = zero, ay = zero, az = zero;
-        const int recs = (lc + 1) >> 1;
-#pragma unroll 4
-        for (int r = 0; r < recs; ++r) {
-            const float4 p0 = lds128(list_addr + 32u * r);
-            const float4 p1 = lds128(list_addr + 32u * r + 16u);
-            group_pair<CLAMP>(f2_pack(p0.x, p0.y), f2_pack(p0.z, p0.w), f2_pack(p1.x, p1.y),
-                              f2_pack(p1.z, p1.w), xi, yi, zi, eps2, ax, ay, az);
+        const int quads = (lc + 3) >> 2;
+#pragma unroll 2
+        for (int r = 0; r < quads; ++r) {
+            const float4 X = lds128(ax_addr + 16u * r);
+            const float4 Y = lds128(ay_addr + 16u * r);
+            const float4 Z = lds128(az_addr + 16u * r);
+            const float4 M = lds128(am_addr + 16u * r);
+            group_pair<CLAMP>(f2_pack(X.x, X.y), f2_pack(Y.x, Y.y), f2_pack(Z.x, Z.y),
+                              f2_pack(M.x, M.y), xi, yi, zi, eps2, ax, ay, az);
+            group_pair<CLAMP>(f2_pack(X.z, X.w), f2_pack(Y.z, Y.w), f2_pack(Z.z, Z.w),
+                              f2_pack(M.z, M.w), xi, yi, zi, eps2, ax, ay, az);
         }
-        f2_two_sum(hx, lx, ax);
-        f2_two_sum(hy, ly, ay);
-        f2_two_sum(hz, lz, az);
+        f2_two_sum(hx, qx, ax);
+        f2_two_sum(hy, qy, ay);
+        f2_two_sum(hz, qz, az);
         inter += (unsigned long long)lc;
         lc = 0;
         __syncwarp();
     };
 
     while (sp > 0) {
-        const int k = min(sp, 32);
-        const bool valid = lane < k;
+        const int k = min(sp, 16);
         int c = 0;
-        if (valid) c = stack[sp - 1 - lane];
+        if (lane < 2 * k) c = 2 * stack[sp - 1 - (lane >> 1)] + (lane & 1);
         __syncwarp();
         sp -= k;
-        tests += (unsigned long long)k;
+        const bool valid = lane < 2 * k && c != 0;
         bool accept = false, open = false;
         float4 nd = make_float4(0.f, 0.f, 0.f, 0.f);
         if (valid) {
@@ -293,28 +301,23 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
                 open = !accept;
             }
         }
+        tests += (unsigned long long)__popc(__ballot_sync(0xffffffffu, valid));
         const unsigned am = __ballot_sync(0xffffffffu, accept);
         const unsigned om = __ballot_sync(0xffffffffu, open);
         if (accept) {
             const int q = lc + __popc(am & lt);
-            PairRec& r = list[q >> 1];
-            const int h = q & 1;
-            r.x[h] = nd.x;
-            r.y[h] = nd.y;
-            r.z[h] = nd.z;
-            r.m[h] = __ldg(&t.nodem[c]);
+            lx[q] = nd.x;
+            ly[q] = nd.y;
+            lz[q] = nd.z;
+            lm[q] = __ldg(&t.nodem[c]);
         }
         lc += __popc(am);
-        const int npush = 2 * __popc(om);
-        if (sp + npush > kGWStack) {  // cannot happen for heaps below 2^40 nodes
+        const int npush = __popc(om);
+        if (sp + npush > kGWStack) {  // more than 32 entries per level of a 2^31-leaf heap
             overflow = true;
             break;
         }
-        if (open) {
-            const int q = sp + 2 * __popc(om & lt);
-            stack[q] = 2 * c + 1;
-            stack[q + 1] = 2 * c;
-        }
+        if (open) stack[sp + __popc(om & lt)] = c;
         sp += npush;
         __syncwarp();
         if (lc > kGWList - 32) evaluate();
@@ -330,13 +333,13 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
         f[n + b] = y[4 * n + b];
         f[2 * n + b] = y[5 * n + b];
         f2_unpack(hx, h0, h1);
-        f2_unpack(lx, l0, l1);
+        f2_unpack(qx, l0, l1);
         f[3 * n + b] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
         f2_unpack(hy, h0, h1);
-        f2_unpack(ly, l0, l1);
+        f2_unpack(qy, l0, l1);
         f[4 * n + b] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
         f2_unpack(hz, h0, h1);
-        f2_unpack(lz, l0, l1);
+        f2_unpack(qz, l0, l1);
         f[5 * n + b] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
     }
     if (lane == 0) {

@@ -27,6 +27,7 @@
 #include "nbg_internal.cuh"
 #include "nbg_ptx.cuh"
 #include "nbg_stats.cuh"
+#include "nbg_tune.cuh"
 
 namespace nbg {
 namespace {
@@ -305,6 +306,67 @@ struct nbg_ensemble {
 
 namespace {
 
+using EnsForce = void (*)(const Body2*, const long long*, const int*, const EnsUnit*, int,
+                          unsigned*, double*, size_t, float);
+
+EnsForce ens_pick(const nbg_ensemble* s) {
+    const bool clamp = !(s->p.softening > 0.0);
+    return clamp ? (s->G == 1 ? ens_force_kernel<true, 1> : ens_force_kernel<true, 2>)
+                 : (s->G == 1 ? ens_force_kernel<false, 1> : ens_force_kernel<false, 2>);
+}
+
+// Work units and launch shape from the tuning keys (the i-block tile of
+// 256 G bodies, CTAs per SM); drops a captured step graph built for an
+// older shape.
+nbg_status ens_configure(nbg_ensemble* s) {
+    nbg_engine* e = s->eng;
+    s->G = (int)std::max<int64_t>(1, std::min<int64_t>(2, e->tune_get("ensemble.pairs_per_lane", 2)));
+    const int blk = kEnsThreads * 2 * s->G;
+    std::vector<EnsUnit> units;
+    for (int sI = 0; sI < s->nsys; ++sI)
+        for (int i0 = 0; i0 < s->h_cnt[sI]; i0 += blk) units.push_back(EnsUnit{sI, i0});
+    // largest systems first (their units cost the most), so the tail of the
+    // persistent launch is made of small units
+    std::stable_sort(units.begin(), units.end(), [&](const EnsUnit& a, const EnsUnit& b) {
+        return s->h_cnt[a.sys] > s->h_cnt[b.sys];
+    });
+    s->nunits = (int)units.size();
+    int occ = 0;
+    NBG_CUDA(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ens_pick(s), kEnsThreads, 0));
+    occ = std::max(occ, 1);
+    const int64_t bps = e->tune_get("ensemble.blocks_per_sm", 0);
+    if (bps > 0 && bps < occ) occ = (int)bps;
+    s->force_grid = (unsigned)std::max(1, std::min(s->nunits, e->sm_count * occ));
+    NBG_CUDA(e, cudaStreamSynchronize(e->stream));
+    cudaFree(s->units);
+    s->units = nullptr;
+    NBG_CUDA(e, cudaMalloc(&s->units, units.size() * sizeof(EnsUnit)));
+    NBG_CUDA(e, cudaMemcpy(s->units, units.data(), units.size() * sizeof(EnsUnit),
+                           cudaMemcpyHostToDevice));
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    if (s->graph_def) cudaGraphDestroy(s->graph_def);
+    s->graph = nullptr;
+    s->graph_def = nullptr;
+    return NBG_OK;
+}
+
+// Stage-0 forces of the current state into k_0 (no host copy).
+nbg_status ens_enqueue_force(nbg_ensemble* s) {
+    nbg_engine* e = s->eng;
+    KPtrs kp;
+    for (int i = 0; i < kStagesRK; ++i) kp.k[i] = s->k[i];
+    const unsigned gv = grid_for(s->B, 256, (unsigned)e->sm_count * 8u);
+    NBG_CUDA(e, cudaMemsetAsync(s->counters, 0, sizeof(unsigned), e->stream));
+    ens_stage_kernel<<<gv, 256, 0, e->stream>>>(0, s->y, s->mass, s->sys, s->dt, kp, s->B,
+                                                s->bodies);
+    NBG_LAUNCHED(e, "ens_stage_kernel");
+    ens_pick(s)<<<s->force_grid, kEnsThreads, 0, e->stream>>>(
+        s->bodies, s->off, s->cnt, s->units, s->nunits, s->counters, s->k[0] + 3 * s->B, s->B,
+        (float)(s->p.softening * s->p.softening));
+    NBG_LAUNCHED(e, "ens_force_kernel");
+    return NBG_OK;
+}
+
 nbg_status ens_enqueue_step(nbg_ensemble* s) {
     nbg_engine* e = s->eng;
     const unsigned gv = grid_for(s->B, 256, (unsigned)e->sm_count * 8u);
@@ -312,10 +374,8 @@ nbg_status ens_enqueue_step(nbg_ensemble* s) {
     for (int i = 0; i < kStagesRK; ++i) kp.k[i] = s->k[i];
     NBG_CUDA(e, cudaMemsetAsync(s->counters, 0, kStagesRK * sizeof(unsigned), e->stream));
     NBG_CUDA(e, cudaMemsetAsync(s->err, 0, s->nsys * sizeof(unsigned long long), e->stream));
-    const bool clamp = !(s->p.softening > 0.0);
     const float eps2 = (float)(s->p.softening * s->p.softening);
-    auto kern = clamp ? (s->G == 1 ? ens_force_kernel<true, 1> : ens_force_kernel<true, 2>)
-                      : (s->G == 1 ? ens_force_kernel<false, 1> : ens_force_kernel<false, 2>);
+    auto kern = ens_pick(s);
     const unsigned grid = s->force_grid;
     for (int st = 0; st < kStagesRK; ++st) {
         ens_stage_kernel<<<gv, 256, 0, e->stream>>>(st, s->y, s->mass, s->sys, s->dt, kp, s->B,
@@ -455,37 +515,17 @@ nbg_status nbg_ensemble_init(nbg_ensemble* s, size_t nsys, const uint32_t* count
             h[d * B + i] = vertices[3 * i + d];
             h[(3 + d) * B + i] = velocities[3 * i + d];
         }
-    s->G = (int)std::max<int64_t>(1, std::min<int64_t>(2, e->tune_get("ensemble.pairs_per_lane", 2)));
-    const int blk = kEnsThreads * 2 * s->G;
-    std::vector<EnsUnit> units;
-    for (size_t sI = 0; sI < nsys; ++sI)
-        for (int i0 = 0; i0 < s->h_cnt[sI]; i0 += blk) units.push_back(EnsUnit{(int)sI, i0});
-    std::stable_sort(units.begin(), units.end(), [&](const EnsUnit& a, const EnsUnit& b) {
-        return s->h_cnt[a.sys] > s->h_cnt[b.sys];
-    });
-    s->nunits = (int)units.size();
-    {
-        const bool clamp = !(s->p.softening > 0.0);
-        auto kern = clamp ? (s->G == 1 ? ens_force_kernel<true, 1> : ens_force_kernel<true, 2>)
-                          : (s->G == 1 ? ens_force_kernel<false, 1> : ens_force_kernel<false, 2>);
-        int occ = 0;
-        NBG_CUDA(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kEnsThreads, 0));
-        s->force_grid = (unsigned)std::max(1, std::min(s->nunits, e->sm_count * std::max(occ, 1)));
-    }
-    NBG_CUDA(e, cudaMalloc(&s->units, units.size() * sizeof(EnsUnit)));
     std::vector<double> dt0(nsys, s->p.dt_initial), t0(nsys, 0.0);
     NBG_CUDA(e, cudaMemcpy(s->off, s->h_off.data(), nsys * sizeof(long long), cudaMemcpyHostToDevice));
     NBG_CUDA(e, cudaMemcpy(s->cnt, s->h_cnt.data(), nsys * sizeof(int), cudaMemcpyHostToDevice));
     NBG_CUDA(e, cudaMemcpy(s->sys, hsys.data(), B * sizeof(int), cudaMemcpyHostToDevice));
     NBG_CUDA(e, cudaMemcpy(s->y, h.data(), B6 * sizeof(double), cudaMemcpyHostToDevice));
     NBG_CUDA(e, cudaMemcpy(s->mass, mass, B * sizeof(double), cudaMemcpyHostToDevice));
-    NBG_CUDA(e, cudaMemcpy(s->units, units.data(), units.size() * sizeof(EnsUnit),
-                           cudaMemcpyHostToDevice));
     NBG_CUDA(e, cudaMemcpy(s->dt, dt0.data(), nsys * sizeof(double), cudaMemcpyHostToDevice));
     NBG_CUDA(e, cudaMemcpy(s->t, t0.data(), nsys * sizeof(double), cudaMemcpyHostToDevice));
     NBG_CUDA(e, cudaMemset(s->accepted, 0, nsys * sizeof(unsigned)));
     NBG_CUDA(e, cudaMemset(s->rejected, 0, nsys * sizeof(unsigned)));
-    return NBG_OK;
+    return ens_configure(s);
 }
 
 nbg_status nbg_ensemble_step(nbg_ensemble* s, int steps) {
@@ -567,19 +607,8 @@ nbg_status nbg_ensemble_fcompute(nbg_ensemble* s, double* f) {
     nbg_engine* e = s->eng;
     if (s->B == 0) return set_error(e, NBG_ERR_NOT_INITIALIZED, "ensemble not initialised");
     // stage 0 of a step: k_0 = [v ; a(y)] of the current state
-    KPtrs kp;
-    for (int i = 0; i < kStagesRK; ++i) kp.k[i] = s->k[i];
-    const unsigned gv = grid_for(s->B, 256, (unsigned)e->sm_count * 8u);
-    NBG_CUDA(e, cudaMemsetAsync(s->counters, 0, sizeof(unsigned), e->stream));
-    ens_stage_kernel<<<gv, 256, 0, e->stream>>>(0, s->y, s->mass, s->sys, s->dt, kp, s->B, s->bodies);
-    NBG_LAUNCHED(e, "ens_stage_kernel");
-    const bool clamp = !(s->p.softening > 0.0);
-    auto kern = clamp ? (s->G == 1 ? ens_force_kernel<true, 1> : ens_force_kernel<true, 2>)
-                      : (s->G == 1 ? ens_force_kernel<false, 1> : ens_force_kernel<false, 2>);
-    kern<<<s->force_grid, kEnsThreads, 0, e->stream>>>(
-        s->bodies, s->off, s->cnt, s->units, s->nunits, s->counters, s->k[0] + 3 * s->B, s->B,
-        (float)(s->p.softening * s->p.softening));
-    NBG_LAUNCHED(e, "ens_force_kernel");
+    nbg_status st = ens_enqueue_force(s);
+    if (st != NBG_OK) return st;
     NBG_CUDA(e, cudaStreamSynchronize(e->stream));
     NBG_CUDA(e, cudaMemcpy(f, s->k[0], 6 * s->B * sizeof(double), cudaMemcpyDeviceToHost));
     return NBG_OK;
@@ -602,7 +631,42 @@ nbg_status nbg_ensemble_statistics(nbg_ensemble* s, double* out) {
 
 nbg_status nbg_ensemble_tune_set(nbg_ensemble* s, const char* key, int64_t value) {
     if (s == nullptr) return NBG_ERR_INVALID_ARG;
-    return nbg_tune_set(s->eng, key, value);
+    nbg_status st = nbg_tune_set(s->eng, key, value);
+    if (st != NBG_OK || s->B == 0) return st;
+    return ens_configure(s);  // takes effect from the next step
+}
+
+nbg_status nbg_ensemble_autotune(nbg_ensemble* s, int reps, char* report, size_t report_len) {
+    if (s == nullptr || reps < 1) return NBG_ERR_INVALID_ARG;
+    nbg_engine* e = s->eng;
+    if (s->B == 0) return set_error(e, NBG_ERR_NOT_INITIALIZED, "ensemble not initialised");
+    NBG_CUDA(e, cudaSetDevice(e->device));
+    const std::map<std::string, int64_t> base = e->tune;
+    std::vector<Candidate> cands;
+    for (int g : {2, 1})
+        for (int bps : {0, 4, 2})
+            cands.push_back({{{"ensemble.pairs_per_lane", g}, {"ensemble.blocks_per_sm", bps}}});
+    std::vector<double> ms;
+    for (const Candidate& c : cands) {
+        e->tune = base;
+        for (const auto& kv : c) e->tune[kv.first] = kv.second;
+        nbg_status st = ens_configure(s);
+        double t = 0.0;
+        if (st == NBG_OK) st = time_enqueue(e, reps, [&]() { return ens_enqueue_force(s); }, &t);
+        if (st != NBG_OK) {
+            e->tune = base;
+            ens_configure(s);
+            return st;
+        }
+        ms.push_back(t);
+    }
+    const size_t best = (size_t)(std::min_element(ms.begin(), ms.end()) - ms.begin());
+    e->tune = base;
+    for (const auto& kv : cands[best]) e->tune[kv.first] = kv.second;
+    nbg_status st = ens_configure(s);
+    if (st != NBG_OK) return st;
+    write_tune_report(e, "ensemble", s->B, reps, cands, ms, best, report, report_len);
+    return NBG_OK;
 }
 
 uint64_t nbg_ensemble_launch_count(const nbg_ensemble* s) {

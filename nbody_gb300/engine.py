@@ -517,6 +517,26 @@ class NbodyEngineGB300:
     def tune_set(self, key: str, value: int) -> None:
         self._check(self._lib.nbg_tune_set(self._h, key.encode(), int(value)), "tune_set")
 
+    def autotune(self, reps: int = 3) -> dict:
+        """nbg_autotune: time every candidate configuration of the force path
+        on the current state, keep the fastest; returns the JSON report."""
+        import json
+        buf = C.create_string_buffer(8192)
+        self._check(self._lib.nbg_autotune(self._h, int(reps), buf, len(buf)), "autotune")
+        return json.loads(buf.value.decode())
+
+    def tune_variant(self) -> str:
+        """Which force path this engine runs (part of the autotuner cache key)."""
+        p = self._params
+        algo = "bh" if p.algo == 1 else "direct"
+        prec = "fp64" if p.precision == 0 else "mixed"
+        return f"{algo}/{prec}/{'soft' if p.softening > 0 else 'clamp'}" + \
+            ("/learned" if p.learned else "")
+
+    @property
+    def device(self) -> int:
+        return int(self._params.device)
+
     def tune_get(self, key: str):
         v = C.c_int64(0)
         st = self._lib.nbg_tune_get(self._h, key.encode(), C.byref(v))

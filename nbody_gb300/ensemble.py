@@ -30,6 +30,8 @@ class Ensemble:
         if st != 0:
             raise NbgError(st, "nbg_ensemble_create failed")
         self._h = h.value
+        self.device = device
+        self.softening = softening
         self.counts = np.zeros(0, dtype=np.uint32)
 
     def _check(self, st: int, what: str) -> None:
@@ -49,6 +51,18 @@ class Ensemble:
 
     def tune_set(self, key: str, value: int) -> None:
         self._check(self._lib.nbg_ensemble_tune_set(self._h, key.encode(), int(value)), "tune_set")
+
+    def autotune(self, reps: int = 3) -> dict:
+        """nbg_ensemble_autotune: force-kernel tile shape and grid, timed on
+        the current state; keeps the fastest; returns the JSON report."""
+        import json
+        buf = C.create_string_buffer(8192)
+        self._check(self._lib.nbg_ensemble_autotune(self._h, int(reps), buf, len(buf)),
+                    "autotune")
+        return json.loads(buf.value.decode())
+
+    def tune_variant(self) -> str:
+        return f"ensemble/{'soft' if self.softening > 0 else 'clamp'}"
 
     def init(self, systems: Sequence) -> None:
         """systems: NBodyData-like objects (vertices, velocities, mass)."""
