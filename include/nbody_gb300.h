@@ -226,7 +226,10 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       "direct.unroll" (2, 4 or 8: j-loop unroll),
  *       "direct.blocks_per_sm" (CTAs per SM of the persistent direct grid),
  *       "bh.walk" (1: group walk with interaction lists, 0: warp-coherent
- *       stackless walk) for the mixed-precision Barnes-Hut path. */
+ *       stackless walk) for the mixed-precision Barnes-Hut path,
+ *       "bh.group" (64 or 32 bodies per warp in the group walk),
+ *       "bh.walk_blocks" (4, 5, 6 or 8: CTAs per SM the group walk's register
+ *       budget is set for). */
 nbg_status nbg_tune_set(nbg_engine* e, const char* key, int64_t value);
 nbg_status nbg_tune_get(nbg_engine* e, const char* key, int64_t* value);
 

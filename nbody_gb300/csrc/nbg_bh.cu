@@ -169,7 +169,9 @@ bh_walk_mixed_kernel(const double* __restrict__ y, double* __restrict__ f, int n
 // four float arrays (x, y, z, m): the stores of one step are consecutive,
 // and one LDS.128 of an array returns two aligned FP32x2 operand pairs.
 // When the list fills, every lane evaluates it for its own body with the
-// direct-sum pair term and folds the result into two-sum accumulators.
+// direct-sum pair term and folds the result into two-sum accumulators; the
+// node loads of the step that finds the list full are issued before that
+// evaluation, which covers their latency.
 // Each body's accepted set refines its per-body set (box distance <= body
 // distance), so the result is at least as accurate as the reference's
 // per-body walk at the same ratio.
@@ -208,21 +210,31 @@ __device__ __forceinline__ void group_pair(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f
     az = f2_fma(dz, s3, az);
 }
 
-template <bool CLAMP>
-__global__ void __launch_bounds__(kGWThreads)
+// BPL bodies per lane: a group of 32 BPL consecutive leaves per warp (lane l
+// holds leaves l, l + 32, ...); every list entry is evaluated for all of them.
+template <bool CLAMP, int MINB, int BPL>
+__global__ void __launch_bounds__(kGWThreads, MINB)
 bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n, float eps2v,
                      TreeState t, unsigned* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     GroupSmem& S = *reinterpret_cast<GroupSmem*>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kGWWarps + warp;
-    if (gw * 32 >= n) return;
-    const int tid = gw * 32 + lane;
-    const bool live = tid < n;
-    const int leaf = n + (live ? tid : gw * 32);
-    const float4 me = __ldg(&t.node4[leaf]);
+    if (gw * 32 * BPL >= n) return;  // n is a power of two >= 32 BPL: groups are full
+    float4 me[BPL];
+#pragma unroll
+    for (int b = 0; b < BPL; ++b) me[b] = __ldg(&t.node4[n + gw * 32 * BPL + b * 32 + lane]);
     // bounding box of the group
-    float lo[3] = {me.x, me.y, me.z}, hi[3] = {me.x, me.y, me.z};
+    float lo[3] = {me[0].x, me[0].y, me[0].z}, hi[3] = {me[0].x, me[0].y, me[0].z};
+#pragma unroll
+    for (int b = 1; b < BPL; ++b) {
+        lo[0] = fminf(lo[0], me[b].x);
+        lo[1] = fminf(lo[1], me[b].y);
+        lo[2] = fminf(lo[2], me[b].z);
+        hi[0] = fmaxf(hi[0], me[b].x);
+        hi[1] = fmaxf(hi[1], me[b].y);
+        hi[2] = fmaxf(hi[2], me[b].z);
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
@@ -239,8 +251,14 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
     const uint32_t az_addr = smem_addr(lz), am_addr = smem_addr(lm);
     const f2_t eps2 = f2_pack(eps2v, eps2v);
     const f2_t zero = f2_pack(0.f, 0.f);
-    const f2_t xi = f2_pack(me.x, me.x), yi = f2_pack(me.y, me.y), zi = f2_pack(me.z, me.z);
-    f2_t hx = zero, hy = zero, hz = zero, qx = zero, qy = zero, qz = zero;
+    f2_t xi[BPL], yi[BPL], zi[BPL], hx[BPL], hy[BPL], hz[BPL], qx[BPL], qy[BPL], qz[BPL];
+#pragma unroll
+    for (int b = 0; b < BPL; ++b) {
+        xi[b] = f2_pack(me[b].x, me[b].x);
+        yi[b] = f2_pack(me[b].y, me[b].y);
+        zi[b] = f2_pack(me[b].z, me[b].z);
+        hx[b] = hy[b] = hz[b] = qx[b] = qy[b] = qz[b] = zero;
+    }
     const unsigned lt = (1u << lane) - 1u;
     unsigned long long tests = 0, inter = 0;
     if (lane == 0) stack[0] = 0;
@@ -258,7 +276,9 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
             lm[lc + lane] = 0.f;
         }
         __syncwarp();
-        f2_t ax = zero, ay = zero, az = zero;
+        f2_t ax[BPL], ay[BPL], az[BPL], bx[BPL], by[BPL], bz[BPL];
+#pragma unroll
+        for (int b = 0; b < BPL; ++b) ax[b] = ay[b] = az[b] = bx[b] = by[b] = bz[b] = zero;
         const int quads = (lc + 3) >> 2;
 #pragma unroll 2
         for (int r = 0; r < quads; ++r) {
@@ -266,14 +286,22 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
             const float4 Y = lds128(ay_addr + 16u * r);
             const float4 Z = lds128(az_addr + 16u * r);
             const float4 M = lds128(am_addr + 16u * r);
-            group_pair<CLAMP>(f2_pack(X.x, X.y), f2_pack(Y.x, Y.y), f2_pack(Z.x, Z.y),
-                              f2_pack(M.x, M.y), xi, yi, zi, eps2, ax, ay, az);
-            group_pair<CLAMP>(f2_pack(X.z, X.w), f2_pack(Y.z, Y.w), f2_pack(Z.z, Z.w),
-                              f2_pack(M.z, M.w), xi, yi, zi, eps2, ax, ay, az);
+#pragma unroll
+            for (int b = 0; b < BPL; ++b) {
+                group_pair<CLAMP>(f2_pack(X.x, X.y), f2_pack(Y.x, Y.y), f2_pack(Z.x, Z.y),
+                                  f2_pack(M.x, M.y), xi[b], yi[b], zi[b], eps2, ax[b], ay[b],
+                                  az[b]);
+                group_pair<CLAMP>(f2_pack(X.z, X.w), f2_pack(Y.z, Y.w), f2_pack(Z.z, Z.w),
+                                  f2_pack(M.z, M.w), xi[b], yi[b], zi[b], eps2, bx[b], by[b],
+                                  bz[b]);
+            }
         }
-        f2_two_sum(hx, qx, ax);
-        f2_two_sum(hy, qy, ay);
-        f2_two_sum(hz, qz, az);
+#pragma unroll
+        for (int b = 0; b < BPL; ++b) {
+            f2_two_sum(hx[b], qx[b], f2_add(ax[b], bx[b]));
+            f2_two_sum(hy[b], qy[b], f2_add(ay[b], by[b]));
+            f2_two_sum(hz[b], qz[b], f2_add(az[b], bz[b]));
+        }
         inter += (unsigned long long)lc;
         lc = 0;
         __syncwarp();
@@ -288,8 +316,13 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
         const bool valid = lane < 2 * k && c != 0;
         bool accept = false, open = false;
         float4 nd = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (valid) {
+        float ndm = 0.f;
+        if (valid) {  // issued before a full list is evaluated, which covers their latency
             nd = __ldg(&t.node4[c]);
+            ndm = __ldg(&t.nodem[c]);
+        }
+        if (lc > kGWList - 32) evaluate();  // room for this step's entries
+        if (valid) {
             if (c >= n) {
                 accept = true;
             } else {
@@ -309,42 +342,42 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
             lx[q] = nd.x;
             ly[q] = nd.y;
             lz[q] = nd.z;
-            lm[q] = __ldg(&t.nodem[c]);
+            lm[q] = ndm;
         }
         lc += __popc(am);
         const int npush = __popc(om);
-        if (sp + npush > kGWStack) {  // more than 32 entries per level of a 2^31-leaf heap
+        if (sp + npush > kGWStack) {  // more than 48 entries per level of a 2^21-leaf heap
             overflow = true;
             break;
         }
         if (open) stack[sp + __popc(om & lt)] = c;
         sp += npush;
         __syncwarp();
-        if (lc > kGWList - 32) evaluate();
     }
     if (overflow) {
         if (lane == 0) atomicOr(err, kDevErrWalkOverflow);
     }
     if (lc > 0) evaluate();
-    if (live) {
+#pragma unroll
+    for (int bb = 0; bb < BPL; ++bb) {
         float h0, h1, l0, l1;
-        const int b = t.body_n[leaf];
+        const int b = t.body_n[n + gw * 32 * BPL + bb * 32 + lane];
         f[b] = y[3 * n + b];
         f[n + b] = y[4 * n + b];
         f[2 * n + b] = y[5 * n + b];
-        f2_unpack(hx, h0, h1);
-        f2_unpack(qx, l0, l1);
+        f2_unpack(hx[bb], h0, h1);
+        f2_unpack(qx[bb], l0, l1);
         f[3 * n + b] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
-        f2_unpack(hy, h0, h1);
-        f2_unpack(qy, l0, l1);
+        f2_unpack(hy[bb], h0, h1);
+        f2_unpack(qy[bb], l0, l1);
         f[4 * n + b] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
-        f2_unpack(hz, h0, h1);
-        f2_unpack(qz, l0, l1);
+        f2_unpack(hz[bb], h0, h1);
+        f2_unpack(qz[bb], l0, l1);
         f[5 * n + b] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
     }
     if (lane == 0) {
         atomicAdd(&t.counters[0], tests);
-        atomicAdd(&t.counters[1], inter * 32ull);
+        atomicAdd(&t.counters[1], inter * 32ull * BPL);
     }
 }
 
@@ -369,11 +402,24 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
     const float eps2 = (float)(e->params.softening * e->params.softening);
     const bool clamp = !(e->params.softening > 0.0);
     if (e->tune_get("bh.walk", 1) == 1 && n >= 32) {
+        // "bh.group": bodies per warp group (32 or 64); "bh.walk_blocks":
+        // CTAs per SM the kernel's register budget is set for (4, 5, 6 or 8:
+        // 128, 102, 80 or 64 registers)
         const size_t smem = sizeof(GroupSmem);
-        auto kern = clamp ? bh_group_walk_kernel<true> : bh_group_walk_kernel<false>;
+        const int bpl = (e->tune_get("bh.group", 64) >= 64 && n >= 64) ? 2 : 1;
+        const int64_t wb = e->tune_get("bh.walk_blocks", bpl == 2 ? 4 : 6);
+        using WalkKernel = void (*)(const double*, double*, int, float, TreeState, unsigned*);
+        WalkKernel kern;
+#define NBG_GW(C, B) (wb >= 8 ? bh_group_walk_kernel<C, 8, B> : wb >= 6 ? bh_group_walk_kernel<C, 6, B> \
+                      : wb >= 5 ? bh_group_walk_kernel<C, 5, B> : bh_group_walk_kernel<C, 4, B>)
+        if (bpl == 2)
+            kern = clamp ? NBG_GW(true, 2) : NBG_GW(false, 2);
+        else
+            kern = clamp ? NBG_GW(true, 1) : NBG_GW(false, 1);
+#undef NBG_GW
         NBG_CUDA(e, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem));
-        const int warps = (n + 31) / 32;
+        const int warps = n / (32 * bpl);
         kern<<<(warps + kGWWarps - 1) / kGWWarps, kGWThreads, smem, e->stream>>>(y, f, n, eps2, *t,
                                                                                 e->d_err);
         NBG_LAUNCHED(e, "bh_group_walk_kernel");

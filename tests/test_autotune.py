@@ -102,7 +102,9 @@ def test_engine_autotune_bh(make_engine):
     e = make_engine(algo="bh", precision="mixed", softening=1e-3, distance_to_node_radius_ratio=2.0)
     assert e.init(d)
     rep = e.autotune(2)
-    assert [c["keys"] for c in rep["candidates"]] == [{"bh.walk": 1}, {"bh.walk": 0}]
+    assert [c["keys"] for c in rep["candidates"]] == [
+        {"bh.walk": 1, "bh.group": g, "bh.walk_blocks": b} for g, b in ((64, 4), (64, 5), (32, 6), (32, 8))
+    ] + [{"bh.walk": 0}]
     assert e.tune_get("bh.walk") == rep["best"]["bh.walk"]
 
 
