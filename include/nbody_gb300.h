@@ -313,6 +313,43 @@ uint64_t nbg_ensemble_launch_count(const nbg_ensemble* s);
 nbg_status nbg_ensemble_profile(nbg_ensemble* s, int enable, double* force_ms,
                                 uint64_t* force_launches);
 
+/* ---- frame stream writer (nbody/nbody_data_stream.cpp) ----
+ * Writes the reference's stream format: <base>.idx (header lines
+ * "#coord_size 8", "#body_count N", "#box_size B", then one
+ * "step<TAB>time<TAB>part<TAB>offset" line per frame), <base><part>.dat
+ * (per frame N vertices then N velocities, 3 doubles per body; a new part
+ * once the current one has reached max_part_size), <base>.col (4 floats per
+ * body) and <base>.mass (N doubles).  Frames of engine state are queued on
+ * the engine stream (transpose to the frame layout + copy into one of two
+ * pinned buffers) and written by a host thread, so file writes overlap the
+ * simulation. */
+typedef struct nbg_stream_writer nbg_stream_writer;
+/* nbody_data_stream::open (nbody/nbody_data_stream.cpp:168-196): makes the
+ * directory, opens part 0 and the index.  e may be NULL (host frames only).
+ * append != 0 continues the stream at <base>: the last part number is read
+ * from its index and no header is written (the reference's append_to). */
+nbg_status nbg_stream_open(nbg_engine* e, const char* base_name, int64_t max_part_size, int append,
+                           nbg_stream_writer** out);
+/* What the reference takes from nbody_data for the header
+ * (nbody/nbody_data_stream.cpp:62-98): body count, box size, colours (4
+ * floats per body; NULL writes zeros) and masses.  Required before writing. */
+nbg_status nbg_stream_set_header(nbg_stream_writer* w, size_t count, uint64_t box_size,
+                                 const float* colors, const double* mass);
+/* nbody_data_stream::write (nbody/nbody_data_stream.cpp:107-160) for the
+ * engine state y (an engine buffer): returns once the frame's copy is queued;
+ * blocks only while both pinned buffers hold frames not yet written.  A
+ * failed asynchronous write is reported by the next write, flush or close. */
+nbg_status nbg_stream_write(nbg_stream_writer* w, const nbg_buffer* y, uint64_t step, double time);
+/* The same for a frame in host memory (vertices and velocities, 3 doubles per
+ * body), written before the call returns. */
+nbg_status nbg_stream_write_host(nbg_stream_writer* w, const double* vertices,
+                                 const double* velocities, uint64_t step, double time);
+/* Waits until every queued frame is on disk. */
+nbg_status nbg_stream_flush(nbg_stream_writer* w);
+/* Flush, close the files and free the writer (nbody_data_stream::close). */
+nbg_status nbg_stream_close(nbg_stream_writer* w);
+const char* nbg_stream_last_error(const nbg_stream_writer* w);
+
 /* FP32 FFMA throughput probe: runs a dependent-chain FMA kernel on the
  * engine's device and returns the measured FP32 FLOP/s (2 per FMA). */
 nbg_status nbg_measure_fp32_peak(nbg_engine* e, double* flops);

@@ -42,7 +42,8 @@ EXPORTS = [
     "nbg_ensemble_synchronize", "nbg_ensemble_status", "nbg_ensemble_get_state",
     "nbg_ensemble_fcompute", "nbg_ensemble_statistics", "nbg_ensemble_tune_set",
     "nbg_ensemble_launch_count", "nbg_ensemble_profile", "nbg_autotune",
-    "nbg_ensemble_autotune",
+    "nbg_ensemble_autotune", "nbg_stream_open", "nbg_stream_set_header", "nbg_stream_write",
+    "nbg_stream_write_host", "nbg_stream_flush", "nbg_stream_close", "nbg_stream_last_error",
 ]
 
 
@@ -175,5 +176,12 @@ def load() -> C.CDLL:
     _proto(lib, "nbg_ensemble_profile", i32, vp, i32, dp, C.POINTER(u64))
     _proto(lib, "nbg_autotune", i32, vp, i32, C.c_char_p, sz)
     _proto(lib, "nbg_ensemble_autotune", i32, vp, i32, C.c_char_p, sz)
+    _proto(lib, "nbg_stream_open", i32, vp, C.c_char_p, C.c_int64, i32, C.POINTER(vp))
+    _proto(lib, "nbg_stream_set_header", i32, vp, sz, u64, vp, vp)
+    _proto(lib, "nbg_stream_write", i32, vp, vp, u64, dbl)
+    _proto(lib, "nbg_stream_write_host", i32, vp, vp, vp, u64, dbl)
+    _proto(lib, "nbg_stream_flush", i32, vp)
+    _proto(lib, "nbg_stream_close", i32, vp)
+    _proto(lib, "nbg_stream_last_error", C.c_char_p, vp)
     _lib = lib
     return lib

@@ -24,11 +24,20 @@ class NBodyData:
     velocities: np.ndarray = field(default_factory=lambda: np.zeros((0, 3)))
     mass: np.ndarray = field(default_factory=lambda: np.zeros(0))
     radius: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    color: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), dtype=np.float32))
     time: float = 0.0
     step: int = 0
     box_size: int = 0
 
     # -- nbody/nbody_data.cpp:176-212 ----------------------------------------
+    def get_color(self) -> np.ndarray:
+        """Colours (N x 4 float32); white where none were given, as the
+        reference's loaders set them (nbody/nbody_data.cpp:508,613)."""
+        n = self.get_count()
+        if self.color.shape != (n, 4):
+            self.color = np.ones((n, 4), dtype=np.float32)
+        return self.color
+
     def get_count(self) -> int:
         return int(self.mass.size)
 
@@ -126,6 +135,15 @@ class NBodyData:
         d.velocities = np.concatenate([p[1] for p in parts])
         d.mass = np.concatenate([p[2] for p in parts])
         d.radius = np.zeros(d.mass.size)
+        # colours of nbody/nbody_data.cpp:278,315-320: the black hole green,
+        # the stars of the two galaxies bluish and reddish
+        k = np.float32(0.8)
+        cols = []
+        for p, c in zip(parts, ((k * 0.5, k * 0.5, k, 1.0), (k, k * 0.5, k * 0.5, 1.0))):
+            col = np.tile(np.array(c, dtype=np.float32), (len(p[2]), 1))
+            col[0] = (0.0, 1.0, 0.0, 1.0)
+            cols.append(col)
+        d.color = np.concatenate(cols).astype(np.float32)
         d.box_size = int(max(max(1.0, sx), max(sy, sz)))
         return d
 

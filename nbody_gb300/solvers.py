@@ -99,15 +99,38 @@ class Solver:
         self.min_step = float(min_step)
         self.max_step = float(max_step)
 
-    def run(self, data, max_time: float, check=None) -> int:
-        """nbody/nbody_solver.cpp:55-105 without the stream dump."""
+    def run(self, data, max_time: float, check=None, stream=None, dump_dt: float = 0.0,
+            check_dt: float = 0.0) -> int:
+        """nbody/nbody_solver.cpp:55-105.  Frames go to `stream` (a
+        nbody_gb300.stream.DataStream) every dump_dt, the first at t = 0; a
+        stream opened on the engine takes them from device memory.  `check`
+        is called every check_dt (every step when check_dt is 0)."""
         dt = self.max_step
+        last_check = data.get_time()
+        last_dump = last_check
+
+        def dump() -> int:
+            if getattr(stream, "_engine", None) is self._engine:
+                return stream.write_engine(self._engine, data)
+            self._engine.get_data(data)
+            return stream.write(data)
+
+        if stream is not None and dump_dt > 0 and last_dump <= 0:
+            if dump() != 0:
+                return -1
+            last_dump = data.get_time()
         while data.get_time() < max_time:
             if self.clamp_to_box:
                 self._engine.clamp(self._engine.get_y(), data.box_size)
             self.advise(dt)
-            if check is not None:
+            t = data.get_time()
+            if check is not None and (check_dt <= 0 or t >= last_check + check_dt - dt * 0.1):
                 check(data)
+                last_check = t
+            if stream is not None and dump_dt > 0 and t >= last_dump + dump_dt - dt * 0.1:
+                if dump() != 0:
+                    return -1
+                last_dump = t
         return 0
 
     def advise(self, dt: float) -> None:
