@@ -113,25 +113,33 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # distributed plumbing (replicas; no data-path collective)
 # ---------------------------------------------------------------------------
-def dist_setup(gpus: int):
+def dist_setup(gpus: int, backend: str = ""):
+    """Rank, local rank and world size from the launcher's environment; one
+    process group (NCCL on GPUs, gloo otherwise) for the barrier and the max
+    over ranks, never for the force data."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if not backend:
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
         return rank, local, world
     return 0, 0, 1
 
 
 def dist_max(x: float, world: int) -> float:
+    """The slowest rank's figure (every rank gets it)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -140,6 +148,13 @@ def barrier(world: int):
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
+
+
+def replica_value(units_per_rank: float, local_ms: float, world: int) -> tuple:
+    """Whole-job throughput of independent replicas: the units all ranks
+    processed over the slowest rank's time.  Returns (value, max ms)."""
+    ms = dist_max(local_ms, world)
+    return world * units_per_rank / (ms * 1e-3), ms
 
 
 # ---------------------------------------------------------------------------
@@ -406,9 +421,8 @@ def run_gb300(args):
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     local_ms = float(np.mean(step_ms))
-    ms = dist_max(local_ms, world)
     pairs_step = 4.0 * n * n
-    value = world * pairs_step / (ms * 1e-3)
+    value, ms = replica_value(pairs_step, local_ms, world)
 
     # ---- kernel-level roofline of the direct kernel ----
     e.profile_enable(True)
