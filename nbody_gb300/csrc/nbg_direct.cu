@@ -444,8 +444,8 @@ __device__ __forceinline__ void sym_issue(float4* tiles, uint64_t* full, int s, 
     bulk_g2s(tiles + s * 2 * kSymT, bodies + (size_t)t * 2 * kSymT, kSymTileBytes, &full[s]);
 }
 
-template <bool CLAMP>
-__global__ void __launch_bounds__(kSymThreads, 4)
+template <bool CLAMP, int MINB>
+__global__ void __launch_bounds__(kSymThreads, MINB)
 direct_sym_kernel(SymArgs a) {
     constexpr int G = kSymG;
     constexpr int kSlots = 6 * G;
@@ -634,7 +634,11 @@ nbg_status direct_sym_launch(nbg_engine* e, const double* y, double* f) {
         y, e->d_mass, bodies, f, n, n_pad);
     NBG_LAUNCHED(e, "pack_sym_kernel");
     const bool clamp = !(e->params.softening > 0.0);
-    auto kern = clamp ? direct_sym_kernel<true> : direct_sym_kernel<false>;
+    // "direct.sym_blocks": CTAs per SM the register budget is set for
+    // (4: 128 registers, 5: 102)
+    const bool b5 = e->tune_get("direct.sym_blocks", 4) >= 5;
+    auto kern = clamp ? (b5 ? direct_sym_kernel<true, 5> : direct_sym_kernel<true, 4>)
+                      : (b5 ? direct_sym_kernel<false, 5> : direct_sym_kernel<false, 4>);
     const size_t smem = sym_smem_bytes();
     NBG_CUDA(e, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));
