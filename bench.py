@@ -230,7 +230,7 @@ def read_traffic():
 
 
 def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 5, walk: int = 1,
-             weights=None):
+             weights=None, order: int = 1):
     """Barnes-Hut fcompute (tree rebuilt every call) at opening ratio lam.
     walk 1 = group walk with interaction lists, 0 = warp-coherent stackless."""
     from nbody_gb300 import _lib
@@ -241,6 +241,7 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
     if e is None:
         return {"unavailable": "engine not created"}
     e.tune_set("bh.walk", walk)
+    e.tune_set("bh.order", order)
     if not e.init(d):
         return {"unavailable": "engine init failed"}
     if weights is not None:
@@ -268,7 +269,7 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
     # node records read by the walk (20 B each: com.xyz + crit^2, mass), per
     # warp test, plus the body rows (16 B in, 24 B out)
     walk_bytes = visits / calls * 20.0 + n_bh * 40.0
-    return {"lambda": lam, "theta": 1.0 / lam, "walk": walk, "learned": learned,
+    return {"lambda": lam, "theta": 1.0 / lam, "walk": walk, "learned": learned, "order": order,
             "bodies_per_s": n_bh / (ms * 1e-3),
             "walk_node_gbs": walk_bytes / (tw / max(nw, 1) * 1e-3) / 1e9,
             "ms_per_fcompute": ms, "wall_ms_per_fcompute": wall * 1e3,
@@ -276,6 +277,41 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
             "p50": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99)),
             "interactions_per_body": inter / calls / n_bh,
             "warp_node_visits_per_warp": visits / calls / (n_bh / 32)}
+
+
+def accuracy_target(n_bh: int, rows, a_ref, d, target: float = 1e-4):
+    """The fastest force path whose p99 relative error on the sampled bodies
+    is at most `target`: Barnes-Hut at growing opening ratios (monopole
+    error falls slowly in the tail) and the direct sum."""
+    from nbody_gb300.engine import create_engine
+    cands = []
+    for order, lams in ((2, (4.0, 8.0, 12.0, 16.0)), (1, (16.0, 32.0, 48.0))):
+        for lam in lams:
+            r = bench_bh(n_bh, lam, False, rows, a_ref, d, calls=2, order=order)
+            cands.append({"path": f"bh {'quadrupole' if order == 2 else 'monopole'} lambda={lam:g}",
+                          "ms": r["ms_per_fcompute"], "p99": r["p99"], "p50": r["p50"]})
+            if r["p99"] <= target:
+                break
+    e = create_engine({"engine": "gb300", "precision": "mixed", "softening": SOFTENING})
+    e.init(d)
+    f = e.create_buffer(8 * 6 * n_bh)
+    e.fcompute(0.0, e.get_y(), f)
+    e.synchronize()
+    t0 = time.perf_counter()
+    e.fcompute(0.0, e.get_y(), f)
+    e.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3
+    out = np.zeros(6 * n_bh)
+    e.read_buffer(out, f)
+    e.close()
+    a = out[3 * n_bh:].reshape(3, n_bh).T[rows]
+    rel = np.linalg.norm(a - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
+    cands.append({"path": "direct (symmetric, FP32 pairs)", "ms": ms,
+                  "p99": float(np.quantile(rel, 0.99))})
+    ok = [c for c in cands if c["p99"] <= target]
+    best = min(ok, key=lambda c: c["ms"]) if ok else None
+    return {"target_p99": target, "candidates": cands,
+            "best": best, "bodies_per_s": n_bh / (best["ms"] * 1e-3) if best else None}
 
 
 def train_correction(epochs: int = 8):
@@ -315,10 +351,13 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20):
            "error_judge": "FP64 direct sum (oracle) on 4096 sampled bodies"}
     res["plain_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d)
     res["plain_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d)
+    res["quadrupole_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, order=2)
+    res["quadrupole_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d, order=2)
     res["coherent_walk_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, walk=0)
     w, fit = train_correction()
     res["learned_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=w)
     res["learned_theta_0.9"]["training"] = fit
+    res["accuracy_target_1e-4"] = accuracy_target(n_bh, rows, a_ref, d)
     p05, l09 = res["plain_theta_0.5"], res["learned_theta_0.9"]
     res["learned_0.9_vs_plain_0.5"] = {
         "bodies_per_s_ratio": l09["bodies_per_s"] / p05["bodies_per_s"],

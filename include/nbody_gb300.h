@@ -230,6 +230,8 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       "bh.walk" (1: group walk with interaction lists, 0: warp-coherent
  *       stackless walk) for the mixed-precision Barnes-Hut path,
  *       "bh.group" (64 or 32 bodies per warp in the group walk),
+ *       "bh.order" (1: monopole cells as the reference; 2: accepted cells
+ *       add their quadrupole term, from FP32 second moments per node),
  *       "bh.walk_blocks" (4, 5, 6 or 8: CTAs per SM the group walk's register
  *       budget is set for). */
 nbg_status nbg_tune_set(nbg_engine* e, const char* key, int64_t value);

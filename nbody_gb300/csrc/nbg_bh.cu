@@ -188,6 +188,51 @@ struct GroupSmem {
     float lm[kGWWarps][kGWList];
 };
 
+// Second list of the quadrupole walk (bh.order = 2): accepted cells with their
+// second moments; leaves stay in the monopole list.  Arrays in the order
+// x, y, z, m, Mxx, Myy, Mzz, tr M / 2, Mxy, Mxz, Myz.
+constexpr int kGWQList = 128;
+constexpr int kGWQFields = 11;
+struct QuadLists {
+    float v[kGWWarps][kGWQFields][kGWQList];
+};
+
+// Monopole plus quadrupole term of a cell (mass centre c, mass m, second
+// central moments M) on a body at x, for two cells at once; d = c - x:
+//   a = d (m / r^3 - 3 k / r^5) - (3 / r^5) M d,  k = tr M / 2 - (5/2) (d.M.d) / r^2,
+// from the expansion of 1 / |r - s| about the mass centre to second order
+// (the first-order term vanishes there).
+template <bool CLAMP>
+__device__ __forceinline__ void quad_pair(const f2_t* q, f2_t xi, f2_t yi, f2_t zi, f2_t eps2,
+                                          f2_t& ax, f2_t& ay, f2_t& az) {
+    const f2_t dx = f2_sub(q[0], xi);
+    const f2_t dy = f2_sub(q[1], yi);
+    const f2_t dz = f2_sub(q[2], zi);
+    f2_t r2 = f2_fma(dz, dz, eps2);
+    r2 = f2_fma(dy, dy, r2);
+    r2 = f2_fma(dx, dx, r2);
+    float r2a, r2b;
+    f2_unpack(r2, r2a, r2b);
+    if (CLAMP) {
+        r2a = fmaxf(r2a, 1e-8f);
+        r2b = fmaxf(r2b, 1e-8f);
+    }
+    const f2_t inv = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
+    const f2_t inv2 = f2_mul(inv, inv);
+    const f2_t inv3 = f2_mul(inv2, inv);
+    const f2_t c3 = f2_mul(f2_mul(inv3, inv2), f2_pack(-3.f, -3.f));  // -3 / r^5
+    // M d with M = [[xx, xy, xz], [xy, yy, yz], [xz, yz, zz]]
+    const f2_t mdx = f2_fma(q[9], dz, f2_fma(q[8], dy, f2_mul(q[4], dx)));
+    const f2_t mdy = f2_fma(q[10], dz, f2_fma(q[5], dy, f2_mul(q[8], dx)));
+    const f2_t mdz = f2_fma(q[6], dz, f2_fma(q[10], dy, f2_mul(q[9], dx)));
+    const f2_t dmd = f2_fma(dz, mdz, f2_fma(dy, mdy, f2_mul(dx, mdx)));
+    const f2_t k = f2_fma(f2_mul(dmd, inv2), f2_pack(-2.5f, -2.5f), q[7]);
+    const f2_t cd = f2_fma(c3, k, f2_mul(q[3], inv3));
+    ax = f2_fma(c3, mdx, f2_fma(cd, dx, ax));
+    ay = f2_fma(c3, mdy, f2_fma(cd, dy, ay));
+    az = f2_fma(c3, mdz, f2_fma(cd, dz, az));
+}
+
 template <bool CLAMP>
 __device__ __forceinline__ void group_pair(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f2_t xi, f2_t yi,
                                            f2_t zi, f2_t eps2, f2_t& ax, f2_t& ay, f2_t& az) {
@@ -212,12 +257,13 @@ __device__ __forceinline__ void group_pair(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f
 
 // BPL bodies per lane: a group of 32 BPL consecutive leaves per warp (lane l
 // holds leaves l, l + 32, ...); every list entry is evaluated for all of them.
-template <bool CLAMP, int MINB, int BPL>
+template <bool CLAMP, int MINB, int BPL, int ORDER>
 __global__ void __launch_bounds__(kGWThreads, MINB)
 bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n, float eps2v,
                      TreeState t, unsigned* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     GroupSmem& S = *reinterpret_cast<GroupSmem*>(smem_raw);
+    QuadLists& Q = *reinterpret_cast<QuadLists*>(smem_raw + sizeof(GroupSmem));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kGWWarps + warp;
     if (gw * 32 * BPL >= n) return;  // n is a power of two >= 32 BPL: groups are full
@@ -307,6 +353,46 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
         __syncwarp();
     };
 
+    int qc = 0;  // entries in the quadrupole list
+    auto evaluate_quad = [&]() {
+        float(*v)[kGWQList] = Q.v[warp];
+        const int pad = (4 - (qc & 3)) & 3;
+        if (lane < pad) {  // massless, momentless padding
+#pragma unroll
+            for (int fld = 0; fld < kGWQFields; ++fld) v[fld][qc + lane] = 0.f;
+        }
+        __syncwarp();
+        const uint32_t base = smem_addr(&v[0][0]);
+        const int quads = (qc + 3) >> 2;
+        f2_t ax[BPL], ay[BPL], az[BPL];
+#pragma unroll
+        for (int b = 0; b < BPL; ++b) ax[b] = ay[b] = az[b] = zero;
+#pragma unroll 1
+        for (int r = 0; r < quads; ++r) {
+            f2_t lo2[kGWQFields], hi2[kGWQFields];
+#pragma unroll
+            for (int fld = 0; fld < kGWQFields; ++fld) {
+                const float4 w = lds128(base + 4u * (uint32_t)(fld * kGWQList) + 16u * r);
+                lo2[fld] = f2_pack(w.x, w.y);
+                hi2[fld] = f2_pack(w.z, w.w);
+            }
+#pragma unroll
+            for (int b = 0; b < BPL; ++b) {
+                quad_pair<CLAMP>(lo2, xi[b], yi[b], zi[b], eps2, ax[b], ay[b], az[b]);
+                quad_pair<CLAMP>(hi2, xi[b], yi[b], zi[b], eps2, ax[b], ay[b], az[b]);
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < BPL; ++b) {
+            f2_two_sum(hx[b], qx[b], ax[b]);
+            f2_two_sum(hy[b], qy[b], ay[b]);
+            f2_two_sum(hz[b], qz[b], az[b]);
+        }
+        inter += (unsigned long long)qc;
+        qc = 0;
+        __syncwarp();
+    };
+
     while (sp > 0) {
         const int k = min(sp, 16);
         int c = 0;
@@ -322,6 +408,7 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
             ndm = __ldg(&t.nodem[c]);
         }
         if (lc > kGWList - 32) evaluate();  // room for this step's entries
+        if (ORDER == 2 && qc > kGWQList - 32) evaluate_quad();
         if (valid) {
             if (c >= n) {
                 accept = true;
@@ -335,9 +422,13 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
             }
         }
         tests += (unsigned long long)__popc(__ballot_sync(0xffffffffu, valid));
-        const unsigned am = __ballot_sync(0xffffffffu, accept);
+        // cells with moments go to the quadrupole list (ORDER 2), the rest
+        // (leaves, or every node for ORDER 1) to the monopole list
+        const bool to_quad = ORDER == 2 && accept && c < n;
+        const bool to_mono = accept && !to_quad;
+        const unsigned am = __ballot_sync(0xffffffffu, to_mono);
         const unsigned om = __ballot_sync(0xffffffffu, open);
-        if (accept) {
+        if (to_mono) {
             const int q = lc + __popc(am & lt);
             lx[q] = nd.x;
             ly[q] = nd.y;
@@ -345,6 +436,27 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
             lm[q] = ndm;
         }
         lc += __popc(am);
+        if (ORDER == 2) {
+            const unsigned aq = __ballot_sync(0xffffffffu, to_quad);
+            if (to_quad) {
+                float(*v)[kGWQList] = Q.v[warp];
+                const int q = qc + __popc(aq & lt);
+                const float4 q0 = __ldg(&t.quad[2 * c]);
+                const float4 q1 = __ldg(&t.quad[2 * c + 1]);
+                v[0][q] = nd.x;
+                v[1][q] = nd.y;
+                v[2][q] = nd.z;
+                v[3][q] = ndm;
+                v[4][q] = q0.x;
+                v[5][q] = q0.y;
+                v[6][q] = q0.z;
+                v[7][q] = q0.w;
+                v[8][q] = q1.x;
+                v[9][q] = q1.y;
+                v[10][q] = q1.z;
+            }
+            qc += __popc(aq);
+        }
         const int npush = __popc(om);
         if (sp + npush > kGWStack) {  // more than 48 entries per level of a 2^21-leaf heap
             overflow = true;
@@ -358,6 +470,7 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
         if (lane == 0) atomicOr(err, kDevErrWalkOverflow);
     }
     if (lc > 0) evaluate();
+    if (ORDER == 2 && qc > 0) evaluate_quad();
 #pragma unroll
     for (int bb = 0; bb < BPL; ++bb) {
         float h0, h1, l0, l1;
@@ -379,6 +492,54 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
         atomicAdd(&t.counters[0], tests);
         atomicAdd(&t.counters[1], inter * 32ull * BPL);
     }
+}
+
+// Second central mass moments per node, bottom-up in FP32 (parallel axis:
+// M = sum over children of M_c + m_c d d^T, d = child centre - node centre);
+// leaves have none.
+__global__ void quad_leaf_kernel(float4* quad, int n) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        quad[2 * (size_t)(n + p)] = make_float4(0.f, 0.f, 0.f, 0.f);
+        quad[2 * (size_t)(n + p) + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+__global__ void quad_level_kernel(int first, TreeState t) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < first; k += gridDim.x * blockDim.x) {
+        const size_t idx = (size_t)first + k;
+        const float4 pc = t.node4[idx];
+        float xx = 0.f, yy = 0.f, zz = 0.f, xy = 0.f, xz = 0.f, yz = 0.f;
+        for (int side = 0; side < 2; ++side) {
+            const size_t c = 2 * idx + side;
+            const float4 cc = t.node4[c];
+            const float mc = t.nodem[c];
+            const float4 q0 = t.quad[2 * c], q1 = t.quad[2 * c + 1];
+            const float dx = cc.x - pc.x, dy = cc.y - pc.y, dz = cc.z - pc.z;
+            xx += q0.x + mc * dx * dx;
+            yy += q0.y + mc * dy * dy;
+            zz += q0.z + mc * dz * dz;
+            xy += q1.x + mc * dx * dy;
+            xz += q1.y + mc * dx * dz;
+            yz += q1.z + mc * dy * dz;
+        }
+        t.quad[2 * idx] = make_float4(xx, yy, zz, 0.5f * (xx + yy + zz));
+        t.quad[2 * idx + 1] = make_float4(xy, xz, yz, 0.f);
+    }
+}
+
+nbg_status tree_quadrupoles(nbg_engine* e) {
+    TreeState* t = e->tree;
+    if (t->quad == nullptr) NBG_CUDA(e, cudaMalloc(&t->quad, 2 * t->size * sizeof(float4)));
+    const int n = (int)t->n;
+    quad_leaf_kernel<<<grid_for(n, 256, (unsigned)e->sm_count * 8u), 256, 0, e->stream>>>(t->quad, n);
+    NBG_LAUNCHED(e, "quad_leaf_kernel");
+    for (int lv = t->levels - 1; lv >= 0; --lv) {
+        const int first = 1 << lv;
+        quad_level_kernel<<<grid_for(first, 256, (unsigned)e->sm_count * 8u), 256, 0, e->stream>>>(
+            first, *t);
+        NBG_LAUNCHED(e, "quad_level_kernel");
+    }
+    return NBG_OK;
 }
 
 }  // namespace
@@ -405,14 +566,23 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
         // "bh.group": bodies per warp group (32 or 64); "bh.walk_blocks":
         // CTAs per SM the kernel's register budget is set for (4, 5, 6 or 8:
         // 128, 102, 80 or 64 registers)
-        const size_t smem = sizeof(GroupSmem);
+        // "bh.order": 1 monopole cells, 2 monopole + quadrupole cells
+        const int order = e->tune_get("bh.order", 1) >= 2 ? 2 : 1;
+        if (order == 2) {
+            nbg_status qs = tree_quadrupoles(e);
+            if (qs != NBG_OK) return qs;
+        }
+        const size_t smem = sizeof(GroupSmem) + (order == 2 ? sizeof(QuadLists) : 0);
         const int bpl = (e->tune_get("bh.group", 64) >= 64 && n >= 64) ? 2 : 1;
         const int64_t wb = e->tune_get("bh.walk_blocks", bpl == 2 ? 4 : 6);
         using WalkKernel = void (*)(const double*, double*, int, float, TreeState, unsigned*);
         WalkKernel kern;
-#define NBG_GW(C, B) (wb >= 8 ? bh_group_walk_kernel<C, 8, B> : wb >= 6 ? bh_group_walk_kernel<C, 6, B> \
-                      : wb >= 5 ? bh_group_walk_kernel<C, 5, B> : bh_group_walk_kernel<C, 4, B>)
-        if (bpl == 2)
+#define NBG_GW(C, B) (wb >= 8 ? bh_group_walk_kernel<C, 8, B, 1> : wb >= 6 ? bh_group_walk_kernel<C, 6, B, 1> \
+                      : wb >= 5 ? bh_group_walk_kernel<C, 5, B, 1> : bh_group_walk_kernel<C, 4, B, 1>)
+        if (order == 2)  // one register budget per group size
+            kern = bpl == 2 ? (clamp ? bh_group_walk_kernel<true, 4, 2, 2> : bh_group_walk_kernel<false, 4, 2, 2>)
+                            : (clamp ? bh_group_walk_kernel<true, 6, 1, 2> : bh_group_walk_kernel<false, 6, 1, 2>);
+        else if (bpl == 2)
             kern = clamp ? NBG_GW(true, 2) : NBG_GW(false, 2);
         else
             kern = clamp ? NBG_GW(true, 1) : NBG_GW(false, 1);

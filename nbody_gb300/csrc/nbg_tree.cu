@@ -428,7 +428,7 @@ void tree_destroy(nbg_engine* e) {
     void* ptrs[] = {t->keys[0], t->keys[1], t->vals[0], t->vals[1], t->lists[0], t->lists[1],
                     t->lists[2], t->spare[0], t->spare[1], t->flag, t->tile_count, t->hist, t->totals,
                     t->com, t->mass, t->bmin, t->bmax, t->crit2, t->body_n, t->node4,
-                    t->nodem, t->feat, t->counters};
+                    t->nodem, t->feat, t->quad, t->counters};
     for (void* p : ptrs) cudaFree(p);
     delete t;
     e->tree = nullptr;

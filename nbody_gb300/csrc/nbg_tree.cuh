@@ -42,6 +42,10 @@ struct TreeState {
     // learned-correction node features (quadrupole, spread), see nbg_learned.cu
     float4* feat = nullptr;   // [3][size] or null
 
+    // quadrupole walk records (nbg_bh.cu): second central mass moments,
+    // quad[2 idx] = (Mxx, Myy, Mzz, tr M / 2), quad[2 idx + 1] = (Mxy, Mxz, Myz, 0)
+    float4* quad = nullptr;   // [2][size] or null
+
     // walk counters: node visits and accepted interactions (mixed walk)
     unsigned long long* counters = nullptr;  // [4]
 };

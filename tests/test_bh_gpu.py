@@ -137,6 +137,34 @@ def test_bh_group_walk_small(make_engine, oracle, n):
     assert np.median(rel) <= np.median(rel_ref)
 
 
+@pytest.mark.parametrize("lam", [2.0, 4.0])
+def test_bh_quadrupole_walk(make_engine, oracle, lam):
+    """bh.order = 2 adds each accepted cell's quadrupole term: the same node
+    tests and interactions as the monopole walk, and a smaller error against
+    the FP64 direct sum (cells' errors fall as (s/d)^3 instead of (s/d)^2)."""
+    n = 16384
+    d = NBodyData.plummer(n, seed=8)
+    y = d.to_state()
+    rows = np.random.default_rng(2).choice(n, size=512, replace=False)
+    a_ref = oracle.accel_rows(y, d.mass, 1e-3, rows=rows)
+    res = {}
+    for order in (1, 2):
+        e = make_engine(algo="bh", precision="mixed", softening=1e-3,
+                        distance_to_node_radius_ratio=lam)
+        e.tune_set("bh.order", order)
+        assert e.init(d)
+        f = _f(e, y)
+        assert np.array_equal(f[:3 * n], y[3 * n:])
+        rel = _rel(f[3 * n:].reshape(3, n).T[rows], a_ref)
+        res[order] = (rel, e.bh_counters())
+    (r1, c1), (r2, c2) = res[1], res[2]
+    print(f"\nlambda {lam}: monopole p50 {np.median(r1):.2e} p99 {np.quantile(r1, 0.99):.2e}; "
+          f"quadrupole p50 {np.median(r2):.2e} p99 {np.quantile(r2, 0.99):.2e}")
+    assert c1 == c2
+    assert np.median(r2) < 0.5 * np.median(r1)
+    assert np.quantile(r2, 0.99) < 0.7 * np.quantile(r1, 0.99)
+
+
 def test_bh_mixed_refit_path(make_engine):
     n = 4096
     d = NBodyData.plummer(n, seed=5)
