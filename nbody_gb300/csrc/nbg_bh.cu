@@ -403,9 +403,14 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
         bool accept = false, open = false;
         float4 nd = make_float4(0.f, 0.f, 0.f, 0.f);
         float ndm = 0.f;
+        float4 nq0 = make_float4(0.f, 0.f, 0.f, 0.f), nq1 = nq0;
         if (valid) {  // issued before a full list is evaluated, which covers their latency
             nd = __ldg(&t.node4[c]);
             ndm = __ldg(&t.nodem[c]);
+            if (ORDER == 2 && c < n) {
+                nq0 = __ldg(&t.quad[2 * c]);
+                nq1 = __ldg(&t.quad[2 * c + 1]);
+            }
         }
         if (lc > kGWList - 32) evaluate();  // room for this step's entries
         if (ORDER == 2 && qc > kGWQList - 32) evaluate_quad();
@@ -441,8 +446,7 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
             if (to_quad) {
                 float(*v)[kGWQList] = Q.v[warp];
                 const int q = qc + __popc(aq & lt);
-                const float4 q0 = __ldg(&t.quad[2 * c]);
-                const float4 q1 = __ldg(&t.quad[2 * c + 1]);
+                const float4 q0 = nq0, q1 = nq1;
                 v[0][q] = nd.x;
                 v[1][q] = nd.y;
                 v[2][q] = nd.z;
@@ -581,7 +585,7 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
                       : wb >= 5 ? bh_group_walk_kernel<C, 5, B, 1> : bh_group_walk_kernel<C, 4, B, 1>)
         if (order == 2)  // one register budget per group size
             kern = bpl == 2 ? (clamp ? bh_group_walk_kernel<true, 4, 2, 2> : bh_group_walk_kernel<false, 4, 2, 2>)
-                            : (clamp ? bh_group_walk_kernel<true, 6, 1, 2> : bh_group_walk_kernel<false, 6, 1, 2>);
+                            : (clamp ? bh_group_walk_kernel<true, 5, 1, 2> : bh_group_walk_kernel<false, 5, 1, 2>);
         else if (bpl == 2)
             kern = clamp ? NBG_GW(true, 2) : NBG_GW(false, 2);
         else

@@ -9,16 +9,32 @@ solver classes drive any engine:
   * rk_butcher     nbody/nbody_solver_rk_butcher.cpp:60-248 (explicit, embedded
                    error = fmaxabs(fmaddn(NULL, k, b2 - b1)), recursive
                    subdivision, optional Kahan correction)
+                   and its implicit branch (:107-130, fixed-point refinement of
+                   the stage derivatives)
   * tables         rkdp (nbody/nbody_solver_rkdp.cpp:30-62),
                    rkck (nbody/nbody_solver_rkck.cpp:30-62),
-                   rkf  (nbody/nbody_solver_rkf.cpp:30-71)
+                   rkf  (nbody/nbody_solver_rkf.cpp:30-71),
+                   rkdverk (nbody/nbody_solver_rkdverk.cpp:29-70),
+                   rkgl (nbody/nbody_solver_rkgl.cpp:29-60, implicit),
+                   rklc (nbody/nbody_solver_rklc.cpp:29-60, implicit)
+  * midpoint       nbody/nbody_solver_midpoint.cpp:23-40
+  * midpoint-st    nbody/nbody_solver_midpoint_stetter.cpp:23-76
+  * trapeze        nbody/nbody_solver_trapeze.cpp:30-56
+  * adams          nbody/nbody_solver_adams.cpp:30-100 (Adams-Bashforth,
+                   rank 1..5, started by another solver)
+  * bs             nbody/nbody_solver_bulirsch_stoer.cpp:7-120 with the Neville
+                   extrapolator (nbody/nbody_extrapolator.cpp:103-181)
   * run loop       nbody/nbody_solver.cpp:55-105 (dt = max_step every advise)
 
-The Butcher coefficients are the published Dormand-Prince, Cash-Karp and
-Fehlberg tables, written out in the same row layout the reference uses.
+The Butcher coefficients are the published Dormand-Prince, Cash-Karp,
+Fehlberg, Verner (DVERK 6(5)), Gauss-Legendre and Lobatto IIIC tables,
+written out in the same row layout the reference uses (the Gauss-Legendre
+entries with the same double expressions in sqrt(15)).  The Feagin 10/12/14
+tables are not restated.
 """
 from __future__ import annotations
 
+import math
 from fractions import Fraction as Fr
 from typing import List, Optional
 
@@ -26,13 +42,14 @@ F8 = 8  # sizeof(nbcoord_t)
 
 
 class ButcherTable:
-    def __init__(self, a, b1, b2, c, embedded=True):
+    def __init__(self, a, b1, b2, c, embedded=True, implicit=False):
         self.steps = len(c)
         self.a = [[float(x) for x in row] for row in a]
         self.b1 = [float(x) for x in b1]
         self.b2 = [float(x) for x in b2]
         self.c = [float(x) for x in c]
         self.embedded = embedded
+        self.implicit = implicit
 
 
 def _t(*rows):
@@ -77,7 +94,39 @@ RKF = ButcherTable(
     [0, Fr(2, 27), Fr(1, 9), Fr(1, 6), Fr(5, 12), Fr(1, 2), Fr(5, 6), Fr(1, 6), Fr(2, 3),
      Fr(1, 3), 1, 0, 1])
 
-TABLES = {"rkdp": RKDP, "rkck": RKCK, "rkf": RKF}
+RKDVERK = ButcherTable(
+    _t([0], [Fr(1, 6)], [Fr(4, 75), Fr(16, 75)], [Fr(5, 6), Fr(-8, 3), Fr(5, 2)],
+       [Fr(-165, 64), Fr(55, 6), Fr(-425, 64), Fr(85, 96)],
+       [Fr(12, 5), -8, Fr(4015, 612), Fr(-11, 36), Fr(88, 255)],
+       [Fr(-8263, 15000), Fr(124, 75), Fr(-643, 680), Fr(-81, 250), Fr(2484, 10625), 0],
+       [Fr(3501, 1720), Fr(-300, 43), Fr(297275, 52632), Fr(-319, 2322), Fr(24068, 84065), 0,
+        Fr(3850, 26703)]),
+    [Fr(3, 40), 0, Fr(875, 2244), Fr(23, 72), Fr(264, 1955), 0, Fr(125, 11592), Fr(43, 616)],
+    [Fr(13, 160), 0, Fr(2375, 5984), Fr(5, 16), Fr(12, 85), Fr(3, 44), 0, 0],
+    [0, Fr(1, 6), Fr(4, 15), Fr(2, 3), Fr(5, 6), 1, Fr(1, 15), 1])
+
+
+def _gauss_legendre3() -> ButcherTable:
+    """3-stage Gauss-Legendre; entries evaluated in double with sqrt(15) as
+    written in the reference table."""
+    r = math.sqrt(15.0)
+    a = [[5.0 / 36.0, 2.0 / 9.0 - r / 15.0, 5.0 / 36.0 - r / 30.0],
+         [5.0 / 36.0 + r / 24.0, 2.0 / 9.0, 5.0 / 36.0 - r / 24.0],
+         [5.0 / 36.0 + r / 30.0, 2.0 / 9.0 + r / 15.0, 5.0 / 36.0]]
+    return ButcherTable(a, [5.0 / 18.0, 4.0 / 9.0, 5.0 / 18.0], [-5.0 / 6.0, 8.0 / 3.0, -5.0 / 6.0],
+                        [0.5 - r / 10.0, 0.5, 0.5 + r / 10.0], embedded=False, implicit=True)
+
+
+RKGL = _gauss_legendre3()
+
+RKLC = ButcherTable(
+    [[Fr(1, 6), Fr(-1, 3), Fr(1, 6)], [Fr(1, 6), Fr(5, 12), Fr(-1, 12)],
+     [Fr(1, 6), Fr(2, 3), Fr(1, 6)]],
+    [Fr(1, 6), Fr(2, 3), Fr(1, 6)], [Fr(-1, 2), 2, Fr(-1, 2)], [0, Fr(1, 2), 1],
+    embedded=True, implicit=True)
+
+TABLES = {"rkdp": RKDP, "rkck": RKCK, "rkf": RKF, "rkdverk": RKDVERK, "rkgl": RKGL,
+          "rklc": RKLC}
 
 
 class Solver:
@@ -183,15 +232,17 @@ class SolverRKButcher(Solver):
     """Explicit embedded Runge-Kutta with recursive step subdivision."""
 
     def __init__(self, table: ButcherTable, error_threshold=1e-4, max_recursion=8,
-                 substep_subdivisions=8, correction=False):
+                 substep_subdivisions=8, correction=False, refine_steps_count=1):
         super().__init__()
         self.bt = table
         self.error_threshold = float(error_threshold)
         self.max_recursion = int(max_recursion)
         self.substep_subdivisions = int(substep_subdivisions)
         self.correction = bool(correction)
+        self.refine_steps_count = int(refine_steps_count)
         self._k: List = []
         self._t = None
+        self._tmpk = None
         self._ystack: List = []
         self._ycorr = None
         self._tcorr = None
@@ -207,6 +258,7 @@ class SolverRKButcher(Solver):
         ps = e.problem_size()
         self._k = e.create_buffers(F8 * ps, self.bt.steps)
         self._t = e.create_buffer(F8 * ps)
+        self._tmpk = e.create_buffer(F8 * ps)
         self._ystack = e.create_buffers(F8 * ps, self.max_recursion)
         if self.correction:
             self._ycorr = e.create_buffer(F8 * ps)
@@ -230,13 +282,35 @@ class SolverRKButcher(Solver):
                 e.fmaddn(self._t, y, self._k, coeff, i)
             e.fcompute(t + bt.c[i] * dt, self._t, self._k[i])
 
+    def _stages_implicit(self, y, t, dt, first_approach):
+        """nbody/nbody_solver_rk_butcher.cpp:107-130: the first call of the
+        solver starts the stage derivatives from an Euler guess; later calls
+        start from the previous step's; then refine_steps_count sweeps of
+        k_i = f(y + dt sum_n a_in k_n)."""
+        e, bt = self._engine, self.bt
+        if first_approach:
+            e.fcompute(t, y, self._tmpk)
+            for i in range(bt.steps):
+                e.fmadd(self._t, y, self._tmpk, dt * bt.c[i])
+                e.fcompute(t + bt.c[i] * dt, self._t, self._k[i])
+        for _ in range(self.refine_steps_count):
+            for i in range(bt.steps):
+                coeff = [dt * bt.a[i][n] for n in range(bt.steps)]
+                e.fmaddn(self._t, y, self._k, coeff, len(self._k))
+                e.fcompute(t + bt.c[i] * dt, self._t, self._k[i])
+
     def _sub_step(self, substeps, t, dt, y, level):
         """nbody/nbody_solver_rk_butcher.cpp:164-248."""
         e, bt = self._engine, self.bt
+        first_approach = False
         if not self._k:
             self._alloc()
+            first_approach = True
         for _ in range(substeps):
-            self._stages(y, t, dt)
+            if bt.implicit:
+                self._stages_implicit(y, t, dt, first_approach)
+            else:
+                self._stages(y, t, dt)
             max_error = 0.0
             if bt.embedded:
                 coeff = [bt.b2[n] - bt.b1[n] for n in range(bt.steps)]
@@ -259,6 +333,236 @@ class SolverRKButcher(Solver):
             t += dt
 
 
+class SolverMidpoint(Solver):
+    """nbody/nbody_solver_midpoint.cpp:23-40."""
+
+    def __init__(self):
+        super().__init__()
+        self._k1 = self._k2 = self._tmp = None
+
+    def advise(self, dt: float) -> None:
+        e = self._engine
+        if self._k1 is None:
+            ps = e.problem_size()
+            self._k1, self._k2, self._tmp = (e.create_buffer(F8 * ps) for _ in range(3))
+        y, t = e.get_y(), e.get_time()
+        e.fcompute(t, y, self._k1)
+        e.fmadd(self._tmp, y, self._k1, dt / 2.0)
+        e.fcompute(t + dt / 2.0, self._tmp, self._k2)
+        e.fmadd_inplace(y, self._k2, dt)
+        e.advise_time(dt)
+
+
+class SolverMidpointStetter(Solver):
+    """Stetter's two-sequence midpoint rule, nbody/nbody_solver_midpoint_stetter.cpp:23-76:
+    u_{k+1} = u_k + dt f(v_k + dt/2 f(u_k)), v_{k+1} = v_k + dt/2 (f(u_k) + f(u_{k+1})),
+    y = (u + v) / 2; f(u_{k+1}) is reused as the next step's f(u_k)."""
+
+    def __init__(self):
+        super().__init__()
+        self._fu: List = []
+        self._uv: List = []
+        self._tmp = self._du = None
+        self._uv_initiated = False
+
+    def reset(self) -> None:
+        self._uv_initiated = False
+
+    def advise(self, dt: float) -> None:
+        e = self._engine
+        y, t = e.get_y(), e.get_time()
+        first = not self._fu
+        if first:
+            ps = e.problem_size()
+            self._tmp = e.create_buffer(F8 * ps)
+            self._du = e.create_buffer(F8 * ps)
+            self._fu = e.create_buffers(F8 * ps, 2)
+            self._uv = e.create_buffers(F8 * ps, 2)
+        if not self._uv_initiated or first:
+            e.copy_buffer(self._uv[0], y)
+            e.copy_buffer(self._uv[1], y)
+            first = True
+            self._uv_initiated = True
+        fu, uv = self._fu, self._uv
+        if first:
+            e.fcompute(t, uv[0], fu[0])
+        e.fmadd(self._tmp, uv[1], fu[0], dt / 2.0)
+        e.fcompute(t + dt / 2.0, self._tmp, self._du)
+        e.fmadd_inplace(uv[0], self._du, dt)
+        e.fcompute(t + dt, uv[0], fu[1])
+        e.fmaddn_inplace(uv[1], fu, [dt / 2.0, dt / 2.0], 2)
+        e.fmaddn(y, None, uv, [0.5, 0.5], len(uv))
+        fu[0], fu[1] = fu[1], fu[0]
+        e.advise_time(dt)
+
+
+class SolverTrapeze(Solver):
+    """nbody/nbody_solver_trapeze.cpp:30-56: Euler predictor, then
+    refine_steps_count corrector sweeps of the trapezoidal rule."""
+
+    def __init__(self, refine_steps_count: int = 1):
+        super().__init__()
+        self.refine_steps_count = int(refine_steps_count)
+        self._f: List = []
+        self._pred = None
+
+    def advise(self, dt: float) -> None:
+        e = self._engine
+        y, t = e.get_y(), e.get_time()
+        if not self._f:
+            ps = e.problem_size()
+            self._f = e.create_buffers(F8 * ps, 2)
+            self._pred = e.create_buffer(F8 * ps)
+        e.fcompute(t, y, self._f[0])
+        e.fmadd(self._pred, y, self._f[0], dt)
+        for sweep in range(self.refine_steps_count + 1):
+            coeff = [dt / 2.0, dt / 2.0]
+            e.fcompute(t, self._pred, self._f[1])
+            if sweep == self.refine_steps_count:
+                e.fmaddn_inplace(y, self._f, coeff, 2)
+            else:
+                e.fmaddn(self._pred, y, self._f, coeff, 2)
+        e.advise_time(dt)
+
+
+_ADAMS = {1: [1.0], 2: [3.0 / 2.0, -1.0 / 2.0], 3: [23.0 / 12.0, -4.0 / 3.0, 5.0 / 12.0],
+          4: [55.0 / 24.0, -59.0 / 24.0, 37.0 / 24.0, -3.0 / 8.0],
+          5: [1901.0 / 720.0, -1387.0 / 360.0, 109.0 / 30.0, -637.0 / 360.0, 251.0 / 720.0]}
+
+
+class SolverAdams(Solver):
+    """Adams-Bashforth of rank 1..5, nbody/nbody_solver_adams.cpp:30-100; the
+    first rank + 1 steps are made by the starter solver while the ring of
+    derivatives fills."""
+
+    def __init__(self, starter: Solver, rank: int = 1, correction: bool = False):
+        super().__init__()
+        self.starter = starter
+        self.rank = int(rank)
+        self.correction = bool(correction)
+        self._f: List = []
+        self._corr = None
+        self._step = 0
+
+    def reset(self) -> None:
+        if self._corr is not None:
+            self._engine.fill_buffer(self._corr, 0.0)
+        self._step = 0
+
+    def advise(self, dt: float) -> None:
+        e = self._engine
+        a = _ADAMS[self.rank]
+        y, t = e.get_y(), e.get_time()
+        fnum = self._step % self.rank
+        if not self._f:
+            self.starter.set_engine(e)
+            self._f = e.create_buffers(F8 * e.problem_size(), self.rank)
+            if self.correction:
+                self._corr = e.create_buffer(F8 * e.problem_size())
+                e.fill_buffer(self._corr, 0.0)
+        if self._step > self.rank:
+            e.fcompute(t, y, self._f[fnum])
+            coeff = [0.0] * self.rank
+            for n in range(self.rank):
+                coeff[(self.rank + fnum - n) % self.rank] = a[n] * dt
+            if self.correction:
+                e.fmaddn_corr(y, self._corr, self._f, coeff, self.rank)
+            else:
+                e.fmaddn_inplace(y, self._f, coeff, self.rank)
+            e.advise_time(dt)
+        else:
+            e.fcompute(t, y, self._f[fnum])
+            self.starter.advise(dt)
+        self._step += 1
+
+
+class NevilleExtrapolator:
+    """nbody/nbody_extrapolator.cpp:103-181: polynomial extrapolation to a zero
+    step in (step count)^order, one table row per level."""
+
+    def __init__(self, engine, order: int, substeps):
+        self.e = engine
+        self.steps = [int(s ** order) if order != 1 else int(s) for s in substeps]
+        ps = engine.problem_size()
+        self.table = engine.create_buffers(F8 * ps, len(substeps))
+        self.prev = engine.create_buffers(F8 * ps, len(substeps))
+        self.diff = engine.create_buffer(F8 * ps)
+
+    def update_table(self, k: int, y) -> None:
+        e = self.e
+        self.table, self.prev = self.prev, self.table
+        e.copy_buffer(self.table[0], y)
+        for j in range(k):
+            s1 = float(self.steps[k])
+            s2 = float(self.steps[k - j - 1])
+            sd = s1 - s2
+            e.fmaddn(self.table[j + 1], None, [self.table[j], self.prev[j]], [s1 / sd, -s2 / sd], 2)
+
+    def estimate_error(self, level: int) -> float:
+        if level == 0:
+            return float("inf")
+        self.e.fmadd(self.diff, self.table[level], self.table[level - 1], -1.0)
+        return self.e.fmaxabs(self.diff)
+
+    def extrapolate(self, level: int, y) -> None:
+        self.e.copy_buffer(y, self.table[level])
+
+
+def _bs_steps(n: int) -> List[int]:
+    """nbody/nbody_solver_bulirsch_stoer.cpp:7-39 (Bulirsch sequence 2, 4, 6, 8, 12, ...)."""
+    steps: List[int] = []
+    if n > 0:
+        steps.append(2)
+    if n > 1:
+        steps.append(4)
+    if n > 2:
+        steps.append(6)
+    for j in range(3, n):
+        steps.append(2 * steps[j - 2])
+    return steps
+
+
+class SolverBulirschStoer(Solver):
+    """nbody/nbody_solver_bulirsch_stoer.cpp:41-120: Stetter midpoint sequences
+    of 2, 4, 6, 8, ... substeps, Neville extrapolation in (substeps)^2, stop at
+    the first level >= 2 whose estimate is below the threshold."""
+
+    def __init__(self, max_level: int = 8, error_threshold: float = 1e-11):
+        super().__init__()
+        self.max_level = int(max_level)
+        self.error_threshold = float(error_threshold)
+        self.sub_steps = _bs_steps(self.max_level)
+        self._y0 = None
+        self._ext = None
+        self._internal = None
+
+    def advise(self, dt: float) -> None:
+        e = self._engine
+        if self._y0 is None:
+            self._y0 = e.create_buffer(F8 * e.problem_size())
+            self._ext = NevilleExtrapolator(e, 2, self.sub_steps)
+            self._internal = SolverMidpointStetter()
+            self._internal.set_engine(e)
+        y, t0 = e.get_y(), e.get_time()
+        e.copy_buffer(self._y0, y)
+        for level in range(self.max_level):
+            e.copy_buffer(y, self._y0)
+            e.set_time(t0)
+            n = self.sub_steps[level]
+            sub_dt = dt / n
+            self._internal.reset()
+            for _ in range(n):
+                self._internal.advise(sub_dt)
+            self._ext.update_table(level, y)
+            if level < 2:
+                continue
+            if self._ext.estimate_error(level) < self.error_threshold or level == self.max_level - 1:
+                self._ext.extrapolate(level, y)
+                break
+        e.set_time(t0)
+        e.advise_time(dt)
+
+
 def create_solver(param: dict) -> Optional[Solver]:
     """nbody_create_solver (nbody/nbody_solvers.cpp:17-110) for the solvers
     restated here; None for an unknown type."""
@@ -272,7 +576,22 @@ def create_solver(param: dict) -> Optional[Solver]:
                             error_threshold=float(param.get("error_threshold", 1e-4)),
                             max_recursion=int(param.get("max_recursion", 8)),
                             substep_subdivisions=int(param.get("substep_subdivisions", 8)),
-                            correction=bool(param.get("correction", False)))
+                            correction=bool(param.get("correction", False)),
+                            refine_steps_count=int(param.get("refine_steps_count", 1)))
+    elif kind == "midpoint":
+        s = SolverMidpoint()
+    elif kind == "midpoint-st":
+        s = SolverMidpointStetter()
+    elif kind == "trapeze":
+        s = SolverTrapeze(int(param.get("refine_steps_count", 1)))
+    elif kind == "adams":
+        starter = create_solver(dict(param, solver=param.get("starter_solver", "euler")))
+        if starter is None:
+            return None
+        s = SolverAdams(starter, int(param.get("rank", 1)), bool(param.get("correction", False)))
+    elif kind == "bs":
+        s = SolverBulirschStoer(int(param.get("max_level", 8)),
+                                float(param.get("error_threshold", 1e-11)))
     else:
         return None
     s.set_time_step(float(param.get("min_step", 1e-9)), float(param.get("max_step", 1e-2)))
