@@ -279,6 +279,46 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
             "warp_node_visits_per_warp": visits / calls / (n_bh / 32)}
 
 
+def bh_rkdp_run(n_bh: int, d, advises: int = 5, dt: float = 1e-3):
+    """SURVEY config 3 as the reference would run it: the rkdp solver
+    (nbody/nbody_solver_rk_butcher.cpp, error threshold 1e-6 on the unscaled
+    max |sum (b2 - b1) k|) driving the Barnes-Hut engine (theta 0.5, tree
+    rebuilt every fcompute) for `advises` advise calls.  The embedded error of
+    FP32 Barnes-Hut forces has a floor near 1e-4 whatever the step, so every
+    step subdivides once (max_recursion 1, 8 substeps) and is accepted at the
+    cap; reported: wall time, fcompute calls, errors seen."""
+    from nbody_gb300.data import NBodyData
+    from nbody_gb300.engine import create_engine
+    from nbody_gb300.solvers import create_solver
+    dd = NBodyData(vertices=d.vertices.copy(), velocities=d.velocities.copy(), mass=d.mass.copy())
+    e = create_engine({"engine": "gb300", "algo": "bh", "precision": "mixed",
+                       "softening": SOFTENING, "distance_to_node_radius_ratio": 2.0,
+                       "tree_layout": "heap_stackless"})
+    e.init(dd)
+    s = create_solver({"solver": "rkdp", "error_threshold": 1e-6, "max_recursion": 1,
+                       "substep_subdivisions": 8})
+    s.set_time_step(1e-9, dt)
+    s.set_engine(e)
+    calls = [0]
+    fc = e.fcompute
+
+    def counted(t, y, f):
+        calls[0] += 1
+        return fc(t, y, f)
+    e.fcompute = counted
+    errs = []
+    t0 = time.perf_counter()
+    for _ in range(advises):
+        s.advise(dt)
+        errs.append(s.last_error)
+    e.synchronize()
+    wall = time.perf_counter() - t0
+    e.close()
+    return {"advises": advises, "dt": dt, "wall_s": wall, "fcompute_calls": calls[0],
+            "bodies_per_s": n_bh * calls[0] / wall, "last_errors": errs,
+            "t_end": dd.get_time()}
+
+
 def accuracy_target(n_bh: int, rows, a_ref, d, target: float = 1e-4):
     """The fastest force path whose p99 relative error on the sampled bodies
     is at most `target`: Barnes-Hut at growing opening ratios (monopole
@@ -358,6 +398,7 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20):
     res["learned_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=w)
     res["learned_theta_0.9"]["training"] = fit
     res["accuracy_target_1e-4"] = accuracy_target(n_bh, rows, a_ref, d)
+    res["rkdp_theta_0.5"] = bh_rkdp_run(n_bh, d)
     p05, l09 = res["plain_theta_0.5"], res["learned_theta_0.9"]
     res["learned_0.9_vs_plain_0.5"] = {
         "bodies_per_s_ratio": l09["bodies_per_s"] / p05["bodies_per_s"],
