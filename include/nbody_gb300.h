@@ -176,6 +176,11 @@ nbg_status nbg_statistics(nbg_engine* e, const nbg_buffer* y, double out[12]);
  * (per warp: every visit is one broadcast node load) and accepted
  * body-node interactions; resets them. */
 nbg_status nbg_bh_counters(nbg_engine* e, uint64_t* visits, uint64_t* interactions);
+/* Deepest per-warp node stack of the group walk since the last
+ * nbg_bh_counters call (which resets it), and the stack capacity of the
+ * current tree (48 entries per level + 32); a walk that would exceed the
+ * capacity stops and reports NBG_ERR_DEVICE_ERROR. */
+nbg_status nbg_bh_stack_peak(nbg_engine* e, uint64_t* peak, uint64_t* capacity);
 /* ---- learned monopole correction (no reference counterpart) ----
  * A 16 -> 64 -> 64 -> 3 GELU MLP (BF16 weights, FP32 accumulate) predicts,
  * for a body-cell interaction accepted at the engine's ratio lambda_l but

@@ -177,16 +177,20 @@ bh_walk_mixed_kernel(const double* __restrict__ y, double* __restrict__ f, int n
 // per-body walk at the same ratio.
 constexpr int kGWWarps = 4;
 constexpr int kGWThreads = kGWWarps * 32;
-constexpr int kGWStack = 1024;  // entries per warp; a walk needs about 32 per tree level
+// Stack entries per warp: 48 per tree level plus 32 (a step pops 16 entries
+// and pushes at most 32), set per launch from the tree depth; the deepest
+// stack of every launch is recorded in counters[2].
+constexpr int kGWStackPerLevel = 48;
 constexpr int kGWList = 256;    // interaction entries per warp
 
-struct GroupSmem {
-    int stack[kGWWarps][kGWStack];
+struct GroupSmem {  // followed by the stacks, kGWWarps x stack_cap ints
     float lx[kGWWarps][kGWList];
     float ly[kGWWarps][kGWList];
     float lz[kGWWarps][kGWList];
     float lm[kGWWarps][kGWList];
 };
+
+inline int group_stack_cap(int levels) { return kGWStackPerLevel * (levels + 1) + 32; }
 
 // Second list of the quadrupole walk (bh.order = 2): accepted cells with their
 // second moments; leaves stay in the monopole list.  Arrays in the order
@@ -260,10 +264,12 @@ __device__ __forceinline__ void group_pair(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f
 template <bool CLAMP, int MINB, int BPL, int ORDER>
 __global__ void __launch_bounds__(kGWThreads, MINB)
 bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n, float eps2v,
-                     TreeState t, unsigned* err) {
+                     TreeState t, int stack_cap, unsigned* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     GroupSmem& S = *reinterpret_cast<GroupSmem*>(smem_raw);
     QuadLists& Q = *reinterpret_cast<QuadLists*>(smem_raw + sizeof(GroupSmem));
+    int* stacks = reinterpret_cast<int*>(smem_raw + sizeof(GroupSmem) +
+                                         (ORDER == 2 ? sizeof(QuadLists) : 0));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kGWWarps + warp;
     if (gw * 32 * BPL >= n) return;  // n is a power of two >= 32 BPL: groups are full
@@ -288,7 +294,7 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
             lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
             hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
         }
-    int* stack = S.stack[warp];
+    int* stack = stacks + warp * stack_cap;
     float* lx = S.lx[warp];
     float* ly = S.ly[warp];
     float* lz = S.lz[warp];
@@ -309,7 +315,7 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
     unsigned long long tests = 0, inter = 0;
     if (lane == 0) stack[0] = 0;
     __syncwarp();
-    int sp = 1, lc = 0;
+    int sp = 1, lc = 0, peak = 1;
     bool overflow = false;
 
     auto evaluate = [&]() {
@@ -462,12 +468,13 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
             qc += __popc(aq);
         }
         const int npush = __popc(om);
-        if (sp + npush > kGWStack) {  // more than 48 entries per level of a 2^21-leaf heap
+        if (sp + npush > stack_cap) {  // beyond 48 entries per level: reported, never written
             overflow = true;
             break;
         }
         if (open) stack[sp + __popc(om & lt)] = c;
         sp += npush;
+        peak = max(peak, sp);
         __syncwarp();
     }
     if (overflow) {
@@ -495,6 +502,7 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
     if (lane == 0) {
         atomicAdd(&t.counters[0], tests);
         atomicAdd(&t.counters[1], inter * 32ull * BPL);
+        atomicMax(&t.counters[2], (unsigned long long)peak);
     }
 }
 
@@ -576,10 +584,12 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
             nbg_status qs = tree_quadrupoles(e);
             if (qs != NBG_OK) return qs;
         }
-        const size_t smem = sizeof(GroupSmem) + (order == 2 ? sizeof(QuadLists) : 0);
+        const int stack_cap = group_stack_cap(t->levels);
+        const size_t smem = sizeof(GroupSmem) + (order == 2 ? sizeof(QuadLists) : 0) +
+                            (size_t)kGWWarps * stack_cap * sizeof(int);
         const int bpl = (e->tune_get("bh.group", 64) >= 64 && n >= 64) ? 2 : 1;
         const int64_t wb = e->tune_get("bh.walk_blocks", bpl == 2 ? 4 : 6);
-        using WalkKernel = void (*)(const double*, double*, int, float, TreeState, unsigned*);
+        using WalkKernel = void (*)(const double*, double*, int, float, TreeState, int, unsigned*);
         WalkKernel kern;
 #define NBG_GW(C, B) (wb >= 8 ? bh_group_walk_kernel<C, 8, B, 1> : wb >= 6 ? bh_group_walk_kernel<C, 6, B, 1> \
                       : wb >= 5 ? bh_group_walk_kernel<C, 5, B, 1> : bh_group_walk_kernel<C, 4, B, 1>)
@@ -594,8 +604,8 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
         NBG_CUDA(e, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem));
         const int warps = n / (32 * bpl);
-        kern<<<(warps + kGWWarps - 1) / kGWWarps, kGWThreads, smem, e->stream>>>(y, f, n, eps2, *t,
-                                                                                e->d_err);
+        kern<<<(warps + kGWWarps - 1) / kGWWarps, kGWThreads, smem, e->stream>>>(
+            y, f, n, eps2, *t, stack_cap, e->d_err);
         NBG_LAUNCHED(e, "bh_group_walk_kernel");
         return NBG_OK;
     }
@@ -624,5 +634,18 @@ extern "C" nbg_status nbg_bh_counters(nbg_engine* e, uint64_t* visits, uint64_t*
     NBG_CUDA(e, cudaMemsetAsync(e->tree->counters, 0, 4 * sizeof(unsigned long long), e->stream));
     if (visits) *visits = h[0];
     if (interactions) *interactions = h[1];
+    return NBG_OK;
+}
+
+extern "C" nbg_status nbg_bh_stack_peak(nbg_engine* e, uint64_t* peak, uint64_t* capacity) {
+    using namespace nbg;
+    if (e == nullptr) return NBG_ERR_INVALID_ARG;
+    if (e->tree == nullptr) return set_error(e, NBG_ERR_NOT_INITIALIZED, "no tree built yet");
+    unsigned long long h = 0;
+    NBG_CUDA(e, cudaMemcpyAsync(&h, e->tree->counters + 2, sizeof(h), cudaMemcpyDeviceToHost,
+                                e->stream));
+    NBG_CUDA(e, cudaStreamSynchronize(e->stream));
+    if (peak) *peak = h;
+    if (capacity) *capacity = (uint64_t)group_stack_cap(e->tree->levels);
     return NBG_OK;
 }

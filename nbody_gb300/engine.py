@@ -432,6 +432,12 @@ class NbodyEngineGB300:
                         "statistics")
         return out
 
+    def bh_stack_peak(self):
+        """(deepest group-walk stack since the last bh_counters, capacity)."""
+        p, c = C.c_uint64(0), C.c_uint64(0)
+        self._check(self._lib.nbg_bh_stack_peak(self._h, C.byref(p), C.byref(c)), "bh_stack_peak")
+        return p.value, c.value
+
     def bh_counters(self):
         """(node visits, interactions) of the mixed Barnes-Hut walk since the last call."""
         v = C.c_uint64(0)

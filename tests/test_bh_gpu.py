@@ -165,6 +165,27 @@ def test_bh_quadrupole_walk(make_engine, oracle, lam):
     assert np.quantile(r2, 0.99) < 0.7 * np.quantile(r1, 0.99)
 
 
+@pytest.mark.parametrize("kind", ["plummer", "cube"])
+@pytest.mark.parametrize("n", [1 << 21, 1 << 22])
+def test_bh_group_walk_deep_trees(make_engine, oracle, n, kind):
+    """Trees of 22 and 23 levels: the group walk's stack stays well inside
+    its capacity (48 entries per level) and the forces keep their accuracy."""
+    d = NBodyData.plummer(n, seed=21) if kind == "plummer" else \
+        NBodyData.uniform_cube(n, side=2.0, seed=21)
+    y = d.to_state()
+    e = make_engine(algo="bh", precision="mixed", softening=1e-3,
+                    distance_to_node_radius_ratio=2.0)
+    assert e.init(d)
+    f = _f(e, y)
+    peak, cap = e.bh_stack_peak()
+    rows = np.random.default_rng(4).choice(n, size=64, replace=False)
+    a_ref = oracle.accel_rows(y, d.mass, 1e-3, rows=rows, nthreads=8)
+    rel = _rel(f[3 * n:].reshape(3, n).T[rows], a_ref)
+    print(f"\n{kind} N={n}: stack peak {peak} of {cap}; p50 {np.median(rel):.2e} max {rel.max():.2e}")
+    assert 0 < peak < cap // 2
+    assert np.all(np.isfinite(f)) and np.median(rel) < 1e-2
+
+
 def test_bh_mixed_refit_path(make_engine):
     n = 4096
     d = NBodyData.plummer(n, seed=5)
