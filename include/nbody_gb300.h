@@ -228,7 +228,8 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  * Keys: "direct.symmetric" (1: each unordered pair evaluated once and
  *       applied to both bodies, the default; 0: one-sided kernel),
  *       "direct.sym_blocks" (4 or 5: CTAs per SM the symmetric kernel's
- *       register budget is set for),
+ *       register budget is set for), "direct.sym_unroll" (1, 2 or 4: unroll
+ *       of its 32-step rotation loop, default 4),
  *       "direct.pairs_per_lane" (2 or 4 packed i-pairs per lane, one-sided),
  *       "direct.unroll" (2, 4 or 8: j-loop unroll),
  *       "direct.blocks_per_sm" (CTAs per SM of the persistent direct grid),

@@ -444,7 +444,7 @@ __device__ __forceinline__ void sym_issue(float4* tiles, uint64_t* full, int s, 
     bulk_g2s(tiles + s * 2 * kSymT, bodies + (size_t)t * 2 * kSymT, kSymTileBytes, &full[s]);
 }
 
-template <bool CLAMP, int MINB>
+template <bool CLAMP, int MINB, int RUNR>
 __global__ void __launch_bounds__(kSymThreads, MINB)
 direct_sym_kernel(SymArgs a) {
     constexpr int G = kSymG;
@@ -562,7 +562,7 @@ direct_sym_kernel(SymArgs a) {
             for (int c = 0; c < kSymT / 32; ++c) {
                 const uint32_t cbase = tbase + (uint32_t)c * 512u;
                 float bx = 0.f, by = 0.f, bz = 0.f;
-#pragma unroll 2
+#pragma unroll RUNR
                 for (int r = 0; r < 32; ++r) {
                     const uint32_t off = cbase + ((uint32_t)((lane + r) & 31) << 4);
                     const float4 p = lds128(off);
@@ -636,9 +636,19 @@ nbg_status direct_sym_launch(nbg_engine* e, const double* y, double* f) {
     const bool clamp = !(e->params.softening > 0.0);
     // "direct.sym_blocks": CTAs per SM the register budget is set for
     // (4: 128 registers, 5: 102)
+    // "direct.sym_unroll": unroll of the 32-step rotation loop (1, 2 or 4)
     const bool b5 = e->tune_get("direct.sym_blocks", 4) >= 5;
-    auto kern = clamp ? (b5 ? direct_sym_kernel<true, 5> : direct_sym_kernel<true, 4>)
-                      : (b5 ? direct_sym_kernel<false, 5> : direct_sym_kernel<false, 4>);
+    const int64_t ru = e->tune_get("direct.sym_unroll", 4);
+    using SymKernel = void (*)(SymArgs);
+    SymKernel kern;
+    if (b5)
+        kern = clamp ? direct_sym_kernel<true, 5, 2> : direct_sym_kernel<false, 5, 2>;
+    else if (ru >= 4)
+        kern = clamp ? direct_sym_kernel<true, 4, 4> : direct_sym_kernel<false, 4, 4>;
+    else if (ru <= 1)
+        kern = clamp ? direct_sym_kernel<true, 4, 1> : direct_sym_kernel<false, 4, 1>;
+    else
+        kern = clamp ? direct_sym_kernel<true, 4, 2> : direct_sym_kernel<false, 4, 2>;
     const size_t smem = sym_smem_bytes();
     NBG_CUDA(e, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));

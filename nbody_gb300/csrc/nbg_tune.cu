@@ -55,6 +55,9 @@ std::vector<Candidate> direct_candidates() {
     for (int bps : {0, 3, 2})
         c.push_back({{"direct.symmetric", 1}, {"direct.sym_blocks", 4}, {"direct.blocks_per_sm", bps}});
     c.push_back({{"direct.symmetric", 1}, {"direct.sym_blocks", 5}, {"direct.blocks_per_sm", 0}});
+    for (int ru : {1, 2})
+        c.push_back({{"direct.symmetric", 1}, {"direct.sym_blocks", 4}, {"direct.sym_unroll", ru},
+                     {"direct.blocks_per_sm", 0}});
     for (int g : {4, 2})
         for (int unr : {2, 4, 8}) {
             if (g == 4 && unr == 8) continue;  // not instantiated
