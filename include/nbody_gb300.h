@@ -239,7 +239,8 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       "bh.order" (1: monopole cells as the reference; 2: accepted cells
  *       add their quadrupole term, from FP32 second moments per node),
  *       "bh.walk_blocks" (4, 5, 6 or 8: CTAs per SM the group walk's register
- *       budget is set for). */
+ *       budget is set for), "bh.eval_unroll" (1, 2 or 4: unroll of the
+ *       interaction-list loop of the 64-body, 4-CTA build). */
 nbg_status nbg_tune_set(nbg_engine* e, const char* key, int64_t value);
 nbg_status nbg_tune_get(nbg_engine* e, const char* key, int64_t* value);
 
@@ -312,7 +313,8 @@ nbg_status nbg_ensemble_fcompute(nbg_ensemble* s, double* f);
  * potential of the ensemble's softening). */
 nbg_status nbg_ensemble_statistics(nbg_ensemble* s, double* out);
 /* Tuning keys "ensemble.pairs_per_lane" (1 or 2: i-tile of 256 or 512 bodies
- * per work unit) and "ensemble.blocks_per_sm" (0 = as many as fit); a change
+ * per work unit), "ensemble.blocks_per_sm" (0 = as many as fit) and
+ * "ensemble.unroll" (2, 4 or 8: j-loop unroll of the force kernel); a change
  * takes effect from the next step (the step graph is captured again). */
 nbg_status nbg_ensemble_tune_set(nbg_ensemble* s, const char* key, int64_t value);
 /* Autotuner of the ensemble force kernel (tile shape and grid), timed on the

@@ -261,7 +261,7 @@ __device__ __forceinline__ void group_pair(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f
 
 // BPL bodies per lane: a group of 32 BPL consecutive leaves per warp (lane l
 // holds leaves l, l + 32, ...); every list entry is evaluated for all of them.
-template <bool CLAMP, int MINB, int BPL, int ORDER>
+template <bool CLAMP, int MINB, int BPL, int ORDER, int EUNR = 2>
 __global__ void __launch_bounds__(kGWThreads, MINB)
 bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n, float eps2v,
                      TreeState t, int stack_cap, unsigned* err) {
@@ -332,7 +332,7 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
 #pragma unroll
         for (int b = 0; b < BPL; ++b) ax[b] = ay[b] = az[b] = bx[b] = by[b] = bz[b] = zero;
         const int quads = (lc + 3) >> 2;
-#pragma unroll 2
+#pragma unroll EUNR
         for (int r = 0; r < quads; ++r) {
             const float4 X = lds128(ax_addr + 16u * r);
             const float4 Y = lds128(ay_addr + 16u * r);
@@ -596,7 +596,12 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
         if (order == 2)  // one register budget per group size
             kern = bpl == 2 ? (clamp ? bh_group_walk_kernel<true, 4, 2, 2> : bh_group_walk_kernel<false, 4, 2, 2>)
                             : (clamp ? bh_group_walk_kernel<true, 5, 1, 2> : bh_group_walk_kernel<false, 5, 1, 2>);
-        else if (bpl == 2)
+        else if (bpl == 2 && wb <= 4 && e->tune_get("bh.eval_unroll", 2) != 2) {
+            // list-evaluation unroll of the default 64-body build
+            const bool u4 = e->tune_get("bh.eval_unroll", 2) >= 4;
+            kern = clamp ? (u4 ? bh_group_walk_kernel<true, 4, 2, 1, 4> : bh_group_walk_kernel<true, 4, 2, 1, 1>)
+                         : (u4 ? bh_group_walk_kernel<false, 4, 2, 1, 4> : bh_group_walk_kernel<false, 4, 2, 1, 1>);
+        } else if (bpl == 2)
             kern = clamp ? NBG_GW(true, 2) : NBG_GW(false, 2);
         else
             kern = clamp ? NBG_GW(true, 1) : NBG_GW(false, 1);

@@ -119,7 +119,7 @@ __device__ __forceinline__ void pair2e(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f2_t 
 
 // Persistent direct sum over all systems.  Each lane holds G packed pairs
 // (2G i-bodies: slots r = 0 .. 2G-1 at i0 + r * 128 + threadIdx.x).
-template <bool CLAMP, int G>
+template <bool CLAMP, int G, int U = 4>
 __global__ void __launch_bounds__(kEnsThreads)
 ens_force_kernel(const Body2* __restrict__ bodies, const long long* __restrict__ off,
                  const int* __restrict__ cnt, const EnsUnit* __restrict__ units, int nunits,
@@ -173,7 +173,7 @@ ens_force_kernel(const Body2* __restrict__ bodies, const long long* __restrict__
 #pragma unroll
             for (int g = 0; g < G; ++g) ax[g] = ay[g] = az[g] = zero;
             const int jn = min(kEnsTile, n - j0);
-#pragma unroll 4
+#pragma unroll U
             for (int j = 0; j < jn; ++j) {
                 const float4 p0 = lds128(tbase + 32u * j);
                 const float4 p1 = lds128(tbase + 32u * j + 16u);
@@ -309,10 +309,18 @@ namespace {
 using EnsForce = void (*)(const Body2*, const long long*, const int*, const EnsUnit*, int,
                           unsigned*, double*, size_t, float);
 
+template <bool CLAMP, int G>
+EnsForce ens_pick_unroll(int64_t u) {
+    return u >= 8 ? ens_force_kernel<CLAMP, G, 8>
+                  : u <= 2 ? ens_force_kernel<CLAMP, G, 2> : ens_force_kernel<CLAMP, G, 4>;
+}
+
+// "ensemble.unroll": unroll of the force kernel's j loop (2, 4 or 8)
 EnsForce ens_pick(const nbg_ensemble* s) {
     const bool clamp = !(s->p.softening > 0.0);
-    return clamp ? (s->G == 1 ? ens_force_kernel<true, 1> : ens_force_kernel<true, 2>)
-                 : (s->G == 1 ? ens_force_kernel<false, 1> : ens_force_kernel<false, 2>);
+    const int64_t u = s->eng->tune_get("ensemble.unroll", 4);
+    return clamp ? (s->G == 1 ? ens_pick_unroll<true, 1>(u) : ens_pick_unroll<true, 2>(u))
+                 : (s->G == 1 ? ens_pick_unroll<false, 1>(u) : ens_pick_unroll<false, 2>(u));
 }
 
 // Work units and launch shape from the tuning keys (the i-block tile of
@@ -646,6 +654,10 @@ nbg_status nbg_ensemble_autotune(nbg_ensemble* s, int reps, char* report, size_t
     for (int g : {2, 1})
         for (int bps : {0, 4, 2})
             cands.push_back({{{"ensemble.pairs_per_lane", g}, {"ensemble.blocks_per_sm", bps}}});
+    for (int g : {2, 1})
+        for (int u : {2, 8})
+            cands.push_back({{{"ensemble.pairs_per_lane", g}, {"ensemble.blocks_per_sm", 0},
+                              {"ensemble.unroll", u}}});
     std::vector<double> ms;
     for (const Candidate& c : cands) {
         e->tune = base;

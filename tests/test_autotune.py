@@ -102,9 +102,12 @@ def test_engine_autotune_bh(make_engine):
     e = make_engine(algo="bh", precision="mixed", softening=1e-3, distance_to_node_radius_ratio=2.0)
     assert e.init(d)
     rep = e.autotune(2)
-    assert [c["keys"] for c in rep["candidates"]] == [
-        {"bh.walk": 1, "bh.group": g, "bh.walk_blocks": b} for g, b in ((64, 4), (64, 5), (32, 6), (32, 8))
-    ] + [{"bh.walk": 0}]
+    keys = [c["keys"] for c in rep["candidates"]]
+    assert keys[:2] == [{"bh.walk": 1, "bh.group": 64, "bh.walk_blocks": b} for b in (4, 5)]
+    assert keys[2:4] == [{"bh.walk": 1, "bh.group": 64, "bh.walk_blocks": 4, "bh.eval_unroll": u}
+                         for u in (1, 4)]
+    assert keys[4:] == [{"bh.walk": 1, "bh.group": 32, "bh.walk_blocks": b} for b in (6, 8)] + \
+        [{"bh.walk": 0}]
     assert e.tune_get("bh.walk") == rep["best"]["bh.walk"]
 
 
@@ -117,7 +120,7 @@ def test_ensemble_autotune_keeps_results():
     ens.init(systems)
     f0 = ens.fcompute()
     rep = ens.autotune(2)
-    assert len(rep["candidates"]) == 6 and rep["best"] in [c["keys"] for c in rep["candidates"]]
+    assert len(rep["candidates"]) == 10 and rep["best"] in [c["keys"] for c in rep["candidates"]]
     f1 = ens.fcompute()
     # another tile shape sums in another order: FP32 rounding only
     scale = np.abs(f0).max()
