@@ -325,7 +325,7 @@ def accuracy_target(n_bh: int, rows, a_ref, d, target: float = 1e-4):
     error falls slowly in the tail) and the direct sum."""
     from nbody_gb300.engine import create_engine
     cands = []
-    for order, lams in ((2, (4.0, 8.0, 12.0, 16.0)), (1, (16.0, 32.0, 48.0))):
+    for order, lams in ((2, (3.0, 3.5, 4.0, 6.0, 8.0)), (1, (16.0, 32.0, 48.0))):
         for lam in lams:
             r = bench_bh(n_bh, lam, False, rows, a_ref, d, calls=2, order=order)
             cands.append({"path": f"bh {'quadrupole' if order == 2 else 'monopole'} lambda={lam:g}",
