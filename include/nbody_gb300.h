@@ -337,7 +337,9 @@ nbg_status nbg_ensemble_profile(nbg_ensemble* s, int enable, double* force_ms,
  * simulation. */
 typedef struct nbg_stream_writer nbg_stream_writer;
 /* nbody_data_stream::open (nbody/nbody_data_stream.cpp:168-196): makes the
- * directory, opens part 0 and the index.  e may be NULL (host frames only).
+ * directory, opens part 0 and the index.  e may be NULL (host frames only);
+ * otherwise the writer uses e's stream and must be closed before e is
+ * destroyed.
  * append != 0 continues the stream at <base>: the last part number is read
  * from its index and no header is written (the reference's append_to). */
 nbg_status nbg_stream_open(nbg_engine* e, const char* base_name, int64_t max_part_size, int append,

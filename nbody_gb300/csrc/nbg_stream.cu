@@ -19,7 +19,6 @@
 // through the same thread, synchronously, which keeps frames in order.
 #include <sys/stat.h>
 
-#include <cerrno>
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
