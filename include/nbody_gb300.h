@@ -239,8 +239,10 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       "bh.order" (1: monopole cells as the reference; 2: accepted cells
  *       add their quadrupole term, from FP32 second moments per node),
  *       "bh.walk_blocks" (4, 5, 6 or 8: CTAs per SM the group walk's register
- *       budget is set for), "bh.eval_unroll" (1, 2 or 4: unroll of the
- *       interaction-list loop of the 64-body, 4-CTA build). */
+ *       budget is set for), "bh.acc_smem" (1: the 64-body walk keeps its
+ *       accumulators in shared memory, the default; 0: in registers),
+ *       "bh.eval_unroll" (1, 2 or 4: unroll of the interaction-list loop of
+ *       the 64-body, register-accumulator, 4-CTA build). */
 nbg_status nbg_tune_set(nbg_engine* e, const char* key, int64_t value);
 nbg_status nbg_tune_get(nbg_engine* e, const char* key, int64_t* value);
 

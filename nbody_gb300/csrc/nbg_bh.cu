@@ -261,7 +261,10 @@ __device__ __forceinline__ void group_pair(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f
 
 // BPL bodies per lane: a group of 32 BPL consecutive leaves per warp (lane l
 // holds leaves l, l + 32, ...); every list entry is evaluated for all of them.
-template <bool CLAMP, int MINB, int BPL, int ORDER, int EUNR = 2>
+// SMACC: the per-body two-sum accumulators (6 BPL packed values per lane)
+// live in shared memory instead of registers; they are touched once per list
+// evaluation, and the registers they free allow more resident warps.
+template <bool CLAMP, int MINB, int BPL, int ORDER, int EUNR = 2, bool SMACC = false>
 __global__ void __launch_bounds__(kGWThreads, MINB)
 bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n, float eps2v,
                      TreeState t, int stack_cap, unsigned* err) {
@@ -270,6 +273,13 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
     QuadLists& Q = *reinterpret_cast<QuadLists*>(smem_raw + sizeof(GroupSmem));
     int* stacks = reinterpret_cast<int*>(smem_raw + sizeof(GroupSmem) +
                                          (ORDER == 2 ? sizeof(QuadLists) : 0));
+    f2_t* acc_sm = reinterpret_cast<f2_t*>(stacks + kGWWarps * stack_cap) + threadIdx.x;
+    f2_t acc_reg[SMACC ? 1 : 6 * BPL];
+    // slot (3 b + component) * 2 + {0: high part, 1: low part}
+    auto slot = [&](int q) -> f2_t& {
+        if constexpr (SMACC) return acc_sm[q * kGWThreads];
+        else return acc_reg[q];
+    };
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kGWWarps + warp;
     if (gw * 32 * BPL >= n) return;  // n is a power of two >= 32 BPL: groups are full
@@ -303,13 +313,14 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
     const uint32_t az_addr = smem_addr(lz), am_addr = smem_addr(lm);
     const f2_t eps2 = f2_pack(eps2v, eps2v);
     const f2_t zero = f2_pack(0.f, 0.f);
-    f2_t xi[BPL], yi[BPL], zi[BPL], hx[BPL], hy[BPL], hz[BPL], qx[BPL], qy[BPL], qz[BPL];
+    f2_t xi[BPL], yi[BPL], zi[BPL];
 #pragma unroll
     for (int b = 0; b < BPL; ++b) {
         xi[b] = f2_pack(me[b].x, me[b].x);
         yi[b] = f2_pack(me[b].y, me[b].y);
         zi[b] = f2_pack(me[b].z, me[b].z);
-        hx[b] = hy[b] = hz[b] = qx[b] = qy[b] = qz[b] = zero;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) slot(6 * b + q) = zero;
     }
     const unsigned lt = (1u << lane) - 1u;
     unsigned long long tests = 0, inter = 0;
@@ -350,9 +361,9 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
         }
 #pragma unroll
         for (int b = 0; b < BPL; ++b) {
-            f2_two_sum(hx[b], qx[b], f2_add(ax[b], bx[b]));
-            f2_two_sum(hy[b], qy[b], f2_add(ay[b], by[b]));
-            f2_two_sum(hz[b], qz[b], f2_add(az[b], bz[b]));
+            f2_two_sum(slot(6 * b + 0), slot(6 * b + 1), f2_add(ax[b], bx[b]));
+            f2_two_sum(slot(6 * b + 2), slot(6 * b + 3), f2_add(ay[b], by[b]));
+            f2_two_sum(slot(6 * b + 4), slot(6 * b + 5), f2_add(az[b], bz[b]));
         }
         inter += (unsigned long long)lc;
         lc = 0;
@@ -390,9 +401,9 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
         }
 #pragma unroll
         for (int b = 0; b < BPL; ++b) {
-            f2_two_sum(hx[b], qx[b], ax[b]);
-            f2_two_sum(hy[b], qy[b], ay[b]);
-            f2_two_sum(hz[b], qz[b], az[b]);
+            f2_two_sum(slot(6 * b + 0), slot(6 * b + 1), ax[b]);
+            f2_two_sum(slot(6 * b + 2), slot(6 * b + 3), ay[b]);
+            f2_two_sum(slot(6 * b + 4), slot(6 * b + 5), az[b]);
         }
         inter += (unsigned long long)qc;
         qc = 0;
@@ -489,14 +500,14 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
         f[b] = y[3 * n + b];
         f[n + b] = y[4 * n + b];
         f[2 * n + b] = y[5 * n + b];
-        f2_unpack(hx[bb], h0, h1);
-        f2_unpack(qx[bb], l0, l1);
+        f2_unpack(slot(6 * bb + 0), h0, h1);
+        f2_unpack(slot(6 * bb + 1), l0, l1);
         f[3 * n + b] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
-        f2_unpack(hy[bb], h0, h1);
-        f2_unpack(qy[bb], l0, l1);
+        f2_unpack(slot(6 * bb + 2), h0, h1);
+        f2_unpack(slot(6 * bb + 3), l0, l1);
         f[4 * n + b] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
-        f2_unpack(hz[bb], h0, h1);
-        f2_unpack(qz[bb], l0, l1);
+        f2_unpack(slot(6 * bb + 4), h0, h1);
+        f2_unpack(slot(6 * bb + 5), l0, l1);
         f[5 * n + b] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
     }
     if (lane == 0) {
@@ -585,10 +596,13 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
             if (qs != NBG_OK) return qs;
         }
         const int stack_cap = group_stack_cap(t->levels);
-        const size_t smem = sizeof(GroupSmem) + (order == 2 ? sizeof(QuadLists) : 0) +
-                            (size_t)kGWWarps * stack_cap * sizeof(int);
+        size_t smem = sizeof(GroupSmem) + (order == 2 ? sizeof(QuadLists) : 0) +
+                      (size_t)kGWWarps * stack_cap * sizeof(int);
         const int bpl = (e->tune_get("bh.group", 64) >= 64 && n >= 64) ? 2 : 1;
-        const int64_t wb = e->tune_get("bh.walk_blocks", bpl == 2 ? 4 : 6);
+        // 64-body groups keep their accumulators in shared memory by default
+        // and run 5 CTAs per SM ("bh.acc_smem" = 0: registers, 4 CTAs)
+        const bool acc_smem = bpl == 2 && order == 1 && e->tune_get("bh.acc_smem", 1) != 0;
+        const int64_t wb = e->tune_get("bh.walk_blocks", bpl == 2 ? (acc_smem ? 5 : 4) : 6);
         using WalkKernel = void (*)(const double*, double*, int, float, TreeState, int, unsigned*);
         WalkKernel kern;
 #define NBG_GW(C, B) (wb >= 8 ? bh_group_walk_kernel<C, 8, B, 1> : wb >= 6 ? bh_group_walk_kernel<C, 6, B, 1> \
@@ -596,7 +610,14 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
         if (order == 2)  // one register budget per group size
             kern = bpl == 2 ? (clamp ? bh_group_walk_kernel<true, 4, 2, 2> : bh_group_walk_kernel<false, 4, 2, 2>)
                             : (clamp ? bh_group_walk_kernel<true, 5, 1, 2> : bh_group_walk_kernel<false, 5, 1, 2>);
-        else if (bpl == 2 && wb <= 4 && e->tune_get("bh.eval_unroll", 2) != 2) {
+        else if (acc_smem) {
+            // accumulators in shared memory (4 or 5 CTAs per SM)
+            smem += (size_t)kGWThreads * 6 * 2 * sizeof(f2_t);
+            kern = clamp ? (wb >= 5 ? bh_group_walk_kernel<true, 5, 2, 1, 2, true>
+                                    : bh_group_walk_kernel<true, 4, 2, 1, 2, true>)
+                         : (wb >= 5 ? bh_group_walk_kernel<false, 5, 2, 1, 2, true>
+                                    : bh_group_walk_kernel<false, 4, 2, 1, 2, true>);
+        } else if (bpl == 2 && wb <= 4 && e->tune_get("bh.eval_unroll", 2) != 2) {
             // list-evaluation unroll of the default 64-body build
             const bool u4 = e->tune_get("bh.eval_unroll", 2) >= 4;
             kern = clamp ? (u4 ? bh_group_walk_kernel<true, 4, 2, 1, 4> : bh_group_walk_kernel<true, 4, 2, 1, 1>)

@@ -83,9 +83,13 @@ extern "C" nbg_status nbg_autotune(nbg_engine* e, int reps, char* report, size_t
     if (e->params.precision == NBG_PREC_FP64 || (e->params.algo == NBG_ALGO_BH && e->params.learned)) {
         cands.push_back({});  // one fixed kernel: nothing to choose
     } else if (e->params.algo == NBG_ALGO_BH) {
-        for (int b : {4, 5}) cands.push_back({{"bh.walk", 1}, {"bh.group", 64}, {"bh.walk_blocks", b}});
+        for (int b : {5, 4})
+            cands.push_back({{"bh.walk", 1}, {"bh.group", 64}, {"bh.walk_blocks", b}, {"bh.acc_smem", 1}});
+        for (int b : {4, 5})
+            cands.push_back({{"bh.walk", 1}, {"bh.group", 64}, {"bh.walk_blocks", b}, {"bh.acc_smem", 0}});
         for (int u : {1, 4})
-            cands.push_back({{"bh.walk", 1}, {"bh.group", 64}, {"bh.walk_blocks", 4}, {"bh.eval_unroll", u}});
+            cands.push_back({{"bh.walk", 1}, {"bh.group", 64}, {"bh.walk_blocks", 4}, {"bh.acc_smem", 0},
+                             {"bh.eval_unroll", u}});
         for (int b : {6, 8}) cands.push_back({{"bh.walk", 1}, {"bh.group", 32}, {"bh.walk_blocks", b}});
         cands.push_back({{"bh.walk", 0}});
     } else {
