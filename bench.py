@@ -201,6 +201,8 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "impl": "reference",
         "config": {"workload": WORKLOAD, "n": args.n,
+                   "precision": "f64 pairs and state (the reference's block engine), "
+                                "reference clamp r^2 >= 1e-8 instead of softening",
                    "cpu": "block engine (nbody/nbody_engine_block.cpp) restated in oracle/, "
                           "OpenMP over host cores; the reference itself needs Qt (absent)"},
         "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
