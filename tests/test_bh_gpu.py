@@ -137,8 +137,9 @@ def test_bh_group_walk_small(make_engine, oracle, n):
     assert np.median(rel) <= np.median(rel_ref)
 
 
+@pytest.mark.parametrize("eps", [1e-3, 0.0])
 @pytest.mark.parametrize("lam", [2.0, 4.0])
-def test_bh_quadrupole_walk(make_engine, oracle, lam):
+def test_bh_quadrupole_walk(make_engine, oracle, lam, eps):
     """bh.order = 2 adds each accepted cell's quadrupole term: the same node
     tests and interactions as the monopole walk, and a smaller error against
     the FP64 direct sum (cells' errors fall as (s/d)^3 instead of (s/d)^2)."""
@@ -146,10 +147,10 @@ def test_bh_quadrupole_walk(make_engine, oracle, lam):
     d = NBodyData.plummer(n, seed=8)
     y = d.to_state()
     rows = np.random.default_rng(2).choice(n, size=512, replace=False)
-    a_ref = oracle.accel_rows(y, d.mass, 1e-3, rows=rows)
+    a_ref = oracle.accel_rows(y, d.mass, eps, rows=rows)
     res = {}
     for order in (1, 2):
-        e = make_engine(algo="bh", precision="mixed", softening=1e-3,
+        e = make_engine(algo="bh", precision="mixed", softening=eps,
                         distance_to_node_radius_ratio=lam)
         e.tune_set("bh.order", order)
         assert e.init(d)

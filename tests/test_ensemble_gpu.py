@@ -46,12 +46,14 @@ def test_ensemble_forces_vs_oracle(gpulib, oracle, eps):
     ens.close()
 
 
-def test_fixed_step_matches_oracle_rkdp(gpulib, oracle):
+@pytest.mark.parametrize("sizes", [[64, 200, 1000], [3000]], ids=["three", "one"])
+def test_fixed_step_matches_oracle_rkdp(gpulib, oracle, sizes):
     """dt_min = dt_max: every attempt is accepted with y += dt sum b2 k; the
     oracle's rkdp with max_recursion 0 does the same step (reference clamp,
-    no softening)."""
+    no softening).  One system is the engine-owned fused RK step: the whole
+    Dormand-Prince step of a single system on the device, one graph."""
     dt = 1e-3
-    sy = _systems([64, 200, 1000], seed=5)
+    sy = _systems(sizes, seed=5)
     ens = Ensemble(softening=0.0, tolerance=1e-30, dt_initial=dt, dt_min=dt, dt_max=dt)
     ens.init(sy)
     ens.step(1)
