@@ -292,3 +292,15 @@ def test_invalid_device_rejected(gpulib):
     from nbody_gb300.engine import create_engine
     for dev in ("-1", "9999"):
         assert create_engine({"engine": "gb300", "device": dev}) is None
+
+
+def test_init_rejects_empty_and_bh_ragged(make_engine):
+    """No bodies is an error (status, message, no state); Barnes-Hut needs a
+    power-of-two body count (the heap's leaves are [N, 2N))."""
+    e = make_engine(precision="fp64")
+    assert not e.init(NBodyData())
+    assert e.last_status == 1  # NBG_ERR_INVALID_ARG
+    b = make_engine(algo="bh", precision="mixed", softening=1e-3)
+    assert not b.init(NBodyData.plummer(1000, seed=1))
+    assert b.last_status == 6  # NBG_ERR_UNSUPPORTED
+    assert b.init(NBodyData.plummer(1024, seed=1))
