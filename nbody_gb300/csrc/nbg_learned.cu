@@ -14,8 +14,10 @@
 //     (bmax - bmin) / (2 s) (3)      box half extents (mass spread)
 //     1 / |u| (1)
 //     (c - box centre) / s (3)       mass-centre offset inside the box
-// The engine generates training samples from its own trees (exact subtree
-// sums over contiguous leaf ranges), trains the network with BF16
+// The network's three outputs are coefficients of the vectors u/|u|,
+// Q u/|u| and the mass-centre offset (apply_head), so its correction turns
+// with the cell.  The engine generates training samples from its own trees
+// (exact subtree sums over contiguous leaf ranges), trains the network with BF16
 // tensor-core forward/backward kernels and Adam, and applies it inside the
 // FP32 walk.  Two inference modes (per-body is the default):
 //   per-body  (learned.group = 0): one MLP sample per (body, cell) pair;
@@ -141,6 +143,35 @@ __device__ __forceinline__ void make_features(float dx, float dy, float dz, floa
     feat[13] = f2.y;
     feat[14] = f2.z;
     feat[15] = f2.w;
+}
+
+// Equivariant output head: the network's three outputs are coefficients of
+// vectors that turn with the cell and the body -- the body direction u/|u|,
+// the quadrupole applied to it Q u/|u|, and the mass-centre offset o:
+//     g = c0 u/|u| + c1 Q u/|u| + c2 o.
+// The exact quadrupole correction has this form, and a bias of the network
+// can no longer point the same way for every cell around a body (where it
+// would add up instead of cancelling).  basis[i] is the i-th vector.
+__device__ __forceinline__ void head_basis(const float feat[16], float basis[3][3]) {
+    const float iu = feat[12];
+    const float ux = feat[0] * iu, uy = feat[1] * iu, uz = feat[2] * iu;
+    // Q = [[xx, xy, xz], [xy, yy, yz], [xz, yz, zz]], feat[3..8] = xx, yy, zz, xy, xz, yz
+    basis[0][0] = ux;
+    basis[0][1] = uy;
+    basis[0][2] = uz;
+    basis[1][0] = fmaf(feat[3], ux, fmaf(feat[6], uy, feat[7] * uz));
+    basis[1][1] = fmaf(feat[6], ux, fmaf(feat[4], uy, feat[8] * uz));
+    basis[1][2] = fmaf(feat[7], ux, fmaf(feat[8], uy, feat[5] * uz));
+    basis[2][0] = feat[13];
+    basis[2][1] = feat[14];
+    basis[2][2] = feat[15];
+}
+
+__device__ __forceinline__ void apply_head(const float feat[16], const float c[3], float g[3]) {
+    float b[3][3];
+    head_basis(feat, b);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) g[k] = fmaf(c[0], b[0][k], fmaf(c[1], b[1][k], c[2] * b[2][k]));
 }
 
 // ---------------------------------------------------------------------------
@@ -344,23 +375,40 @@ train_kernel(const float* __restrict__ x, const float* __restrict__ tg, const in
         }
         float out[2][4];
         layer_out(a2, S.frag, S.bias, lane, out);
-        // ---- loss gradient dY = 2 (Y - T) / B, rows = samples ----
+        // ---- loss gradient through the head, rows = samples ----
+        // g = sum_i c_i b_i, loss = |g - T|^2, dL/dc_i = 2 (g - T) . b_i / B.
+        // Lane (g, t) of a row quad holds output columns 2t, 2t+1 of rows g
+        // and g + 8: c0, c1 on t = 0 and c2 on t = 1; every lane of the quad
+        // gathers the three, evaluates the head and keeps its own columns.
         float d3[2][1][4];
         for (int m = 0; m < 2; ++m)
             for (int h = 0; h < 2; ++h) {  // h: row g or g + 8
                 const size_t s = ch * 32 + 16 * m + g + 8 * h;
                 const bool sl = s < bsize;
                 const size_t srow = sl ? (size_t)order[b0 + s] : 0;
-                for (int j = 0; j < 2; ++j) {
-                    const int col = 2 * t + j;
-                    float d = 0.f;
-                    if (sl && col < kOut) {
-                        const float e = out[m][2 * h + j] - tg[srow * 4 + col];
-                        sq += (double)e * e;
-                        d = 2.f * e * inv_b;
-                    }
-                    d3[m][0][2 * h + j] = d;
+                float c[3];
+                c[0] = __shfl_sync(0xffffffffu, out[m][2 * h], lane & ~3);
+                c[1] = __shfl_sync(0xffffffffu, out[m][2 * h + 1], lane & ~3);
+                c[2] = __shfl_sync(0xffffffffu, out[m][2 * h], (lane & ~3) | 1);
+                float dc[4] = {0.f, 0.f, 0.f, 0.f};
+                if (sl) {
+                    float fe[16];
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) fe[k] = x[srow * 16 + k];
+                    float b[3][3], gp[3];
+                    head_basis(fe, b);
+                    apply_head(fe, c, gp);
+                    float e[3];
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) e[k] = gp[k] - tg[srow * 4 + k];
+                    if (t == 0) sq += (double)e[0] * e[0] + (double)e[1] * e[1] + (double)e[2] * e[2];
+#pragma unroll
+                    for (int i = 0; i < 3; ++i)
+                        dc[i] = 2.f * inv_b * fmaf(e[0], b[i][0], fmaf(e[1], b[i][1], e[2] * b[i][2]));
                 }
+                const int col = 2 * t;
+                d3[m][0][2 * h] = col < kOut ? dc[col] : 0.f;
+                d3[m][0][2 * h + 1] = col + 1 < kOut ? dc[col + 1] : 0.f;
             }
         stage_T<1>(W.d3T, d3, lane);
         __syncwarp();
@@ -620,8 +668,9 @@ learned_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n,
         const float inv_s = 1.f / s;
         make_features(nd.x - cx, nd.y - cy, nd.z - cz, inv_s, __ldg(&t.feat[3 * node]),
                       __ldg(&t.feat[3 * node + 1]), __ldg(&t.feat[3 * node + 2]), feat);
-        float g[3];
-        mlp::infer_warp(feat, g, S.frag, S.bias, S.xs[warp], S.os[warp], lane);
+        float cg[3], g[3];
+        mlp::infer_warp(feat, cg, S.frag, S.bias, S.xs[warp], S.os[warp], lane);
+        apply_head(feat, cg, g);
         if (have) {
             const float k = __ldg(&t.nodem[node]) * inv_s * inv_s;
             corr[0] = k * g[0];
@@ -673,8 +722,9 @@ learned_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n,
                         make_features(dx, dy, dz, inv_s, __ldg(&t.feat[3 * curr]),
                                       __ldg(&t.feat[3 * curr + 1]), __ldg(&t.feat[3 * curr + 2]),
                                       feat);
-                        float g[3];
-                        mlp::infer_warp(feat, g, S.frag, S.bias, S.xs[warp], S.os[warp], lane);
+                        float cg[3], g[3];
+                        mlp::infer_warp(feat, cg, S.frag, S.bias, S.xs[warp], S.os[warp], lane);
+                        apply_head(feat, cg, g);
                         if (band) {
                             const float k = __ldg(&t.nodem[curr]) * inv_s * inv_s;
                             ax = fmaf(k, g[0], ax);

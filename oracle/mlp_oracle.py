@@ -6,9 +6,13 @@ nbg_learned.cu).  The correction has no counterpart in the reference.
 
 Network 16 -> 64 -> 64 -> 3, GELU in the tanh form
 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))) (Hendrycks & Gimpel 2016)
-after both hidden layers; loss = sum over samples and outputs of the squared
-error, gradients of the mean loss (sum / count).  Parameter layout (flat,
-k-major): W1[16][64], b1[64], W2[64][64], b2[64], W3[64][3], b3[3].
+after both hidden layers.  The three outputs c are coefficients of vectors
+built from the sample's features x (the engine's head, apply_head in
+nbg_learned.cu): g = c0 u/|u| + c1 Q u/|u| + c2 o, with u = x[0:3],
+1/|u| = x[12], Q the symmetric matrix of x[3:9] (xx, yy, zz, xy, xz, yz) and
+o = x[13:16].  loss = sum over samples of |g - t|^2, gradients of the mean
+loss (sum / count).  Parameter layout (flat, k-major): W1[16][64], b1[64],
+W2[64][64], b2[64], W3[64][3], b3[3].
 """
 from __future__ import annotations
 
@@ -50,6 +54,22 @@ def forward(w, x):
     return a2 @ W3 + b3
 
 
+def basis(x):
+    """[B, 3, 3]: basis[s, i] is the i-th head vector of sample s."""
+    x = np.asarray(x, dtype=np.float64)
+    uh = x[:, 0:3] * x[:, 12:13]
+    xx, yy, zz, xy, xz, yz = (x[:, k] for k in range(3, 9))
+    qu = np.stack([xx * uh[:, 0] + xy * uh[:, 1] + xz * uh[:, 2],
+                   xy * uh[:, 0] + yy * uh[:, 1] + yz * uh[:, 2],
+                   xz * uh[:, 0] + yz * uh[:, 1] + zz * uh[:, 2]], axis=1)
+    return np.stack([uh, qu, x[:, 13:16]], axis=1)
+
+
+def head(x, c):
+    """g = sum_i c_i basis_i (the correction in units of m / s^2)."""
+    return np.einsum("si,sik->sk", np.asarray(c, dtype=np.float64), basis(x))
+
+
 def loss_grad(w, x, t):
     """(sum of squared errors, gradient of the mean loss)."""
     x = np.asarray(x, dtype=np.float64)
@@ -60,9 +80,10 @@ def loss_grad(w, x, t):
     a1 = gelu(z1)
     z2 = a1 @ W2 + b2
     a2 = gelu(z2)
-    y = a2 @ W3 + b3
-    e = y - t
-    dy = 2.0 * e / B
+    c = a2 @ W3 + b3
+    bs = basis(x)
+    e = np.einsum("si,sik->sk", c, bs) - t
+    dy = np.einsum("sk,sik->si", 2.0 * e / B, bs)
     g = np.zeros(N_PARAMS)
     g[OFF_W3:OFF_B3] = (a2.T @ dy).ravel()
     g[OFF_B3:N_PARAMS] = dy.sum(axis=0)

@@ -162,10 +162,11 @@ def test_inference_path_matches_fp64_forward(make_engine, trained):
 @pytest.mark.parametrize("group", [0, 1])
 def test_learned_walk_vs_plain(make_engine, oracle, trained, group):
     """What the trained network changes in the force at theta = 0.9, judged by
-    the FP64 direct sum on a snapshot the network never saw.  Recorded, with
-    theta = 0.5 beside it; the assertions cover what must hold: finite forces
-    and velocity rows copied exactly, and the learned walk visiting the same
-    nodes as the plain walk at the same ratio."""
+    the FP64 direct sum on a snapshot the network never saw, with theta = 0.5
+    beside it.  Per-body inference (group 0) must lower the median and p99
+    errors of plain theta = 0.9; the warp-centroid mode (group 1) is recorded.
+    Both: finite forces, velocity rows copied exactly, and the learned walk
+    visiting the same nodes as the plain walk at the same ratio."""
     w = trained[0]
     n = 1 << 15
     d = NBodyData.plummer(n, seed=77)
@@ -194,4 +195,8 @@ def test_learned_walk_vs_plain(make_engine, oracle, trained, group):
     print(f"\ngroup={group}: plain theta0.9 {q(plain09)} | learned theta0.9 {q(learn09)} | "
           f"plain theta0.5 {q(plain05)}")
     assert c0 == c1  # same walk: the correction adds work, never changes the visit sequence
-    assert np.median(learn09) < 10 * np.median(plain09)
+    if group == 0:
+        assert np.median(learn09) < 0.95 * np.median(plain09)
+        assert np.quantile(learn09, 0.99) < 0.95 * np.quantile(plain09, 0.99)
+    else:
+        assert np.median(learn09) < 10 * np.median(plain09)
