@@ -318,7 +318,8 @@ __device__ __forceinline__ void acc_colsum(float* gacc, int off, int cmax, const
 __global__ void __launch_bounds__(kTrainWarps * 32)
 train_kernel(const float* __restrict__ x, const float* __restrict__ tg, const int* __restrict__ order,
              size_t b0, size_t bsize, const uint2* __restrict__ frag_g,
-             const float* __restrict__ bias_g, float* __restrict__ grad, double* __restrict__ loss) {
+             const float* __restrict__ bias_g, float* __restrict__ grad, double* __restrict__ loss,
+             float wnorm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
     for (int i = threadIdx.x; i < kFragWords; i += blockDim.x) S.frag[i] = frag_g[i];
@@ -401,10 +402,17 @@ train_kernel(const float* __restrict__ x, const float* __restrict__ tg, const in
                     float e[3];
 #pragma unroll
                     for (int k = 0; k < 3; ++k) e[k] = gp[k] - tg[srow * 4 + k];
-                    if (t == 0) sq += (double)e[0] * e[0] + (double)e[1] * e[1] + (double)e[2] * e[2];
+                    // weighted loss: the squared error in force units, (m / s^2)^2
+                    // |g - T|^2, normalised to a mean weight of 1 (wnorm > 0)
+                    const float ws = tg[srow * 4 + 3];
+                    const float fac = wnorm > 0.f ? ws * ws * wnorm : 1.f;
+                    if (t == 0)
+                        sq += (double)fac * ((double)e[0] * e[0] + (double)e[1] * e[1] +
+                                             (double)e[2] * e[2]);
 #pragma unroll
                     for (int i = 0; i < 3; ++i)
-                        dc[i] = 2.f * inv_b * fmaf(e[0], b[i][0], fmaf(e[1], b[i][1], e[2] * b[i][2]));
+                        dc[i] = 2.f * inv_b * fac *
+                                fmaf(e[0], b[i][0], fmaf(e[1], b[i][1], e[2] * b[i][2]));
                 }
                 const int col = 2 * t;
                 d3[m][0][2 * h] = col < kOut ? dc[col] : 0.f;
@@ -596,7 +604,7 @@ __global__ void sample_targets_kernel(const int* __restrict__ pairs, size_t npai
     to[4 * w + 0] = (float)((ex - cx * sm) * scale);
     to[4 * w + 1] = (float)((ey - cy * sm) * scale);
     to[4 * w + 2] = (float)((ez - cz * sm) * scale);
-    to[4 * w + 3] = 0.f;
+    to[4 * w + 3] = (float)(m / (s * s));  // force scale of the cell (training weight)
     const float4 nd = t.node4[node];
     const float4 me = t.node4[leaf];
     float feat[16];
@@ -1025,7 +1033,7 @@ nbg_status nbg_learn_clear_samples(nbg_engine* e) {
 // One pass of forward + backward over `order[b0 .. b0 + bsize)` of (x, t);
 // grad and loss accumulate on the device.
 static nbg_status run_train_pass(nbg_engine* e, const float* x, const float* t, const int* order,
-                                 size_t b0, size_t bsize) {
+                                 size_t b0, size_t bsize, float wnorm = 0.f) {
     LearnState* L = e->learn;
     const size_t smem = train_smem();
     NBG_CUDA(e, cudaFuncSetAttribute(train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1035,7 +1043,7 @@ static nbg_status run_train_pass(nbg_engine* e, const float* x, const float* t, 
                                                (size_t)e->sm_count);
     if (grid < 1) grid = 1;
     train_kernel<<<grid, kTrainWarps * 32, smem, e->stream>>>(x, t, order, b0, bsize, L->frag,
-                                                             L->bias, L->grad, L->loss);
+                                                             L->bias, L->grad, L->loss, wnorm);
     NBG_LAUNCHED(e, "train_kernel");
     return NBG_OK;
 }
@@ -1086,6 +1094,19 @@ nbg_status nbg_learn_train(nbg_engine* e, int epochs, size_t batch, double lr, u
         const size_t j = (size_t)((st >> 33) % (uint64_t)(i + 1));
         std::swap(perm[i], perm[j]);
     }
+    // "learned.weighted": weight each sample's squared error by its cell's
+    // force scale (m / s^2)^2, normalised over the training set
+    float wnorm = 0.f;
+    if (e->tune_get("learned.weighted", 0) != 0) {
+        std::vector<float> ht(4 * total);
+        NBG_CUDA(e, cudaMemcpy(ht.data(), L->t, 4 * total * sizeof(float), cudaMemcpyDeviceToHost));
+        double sw = 0.0;
+        for (size_t i = 0; i < ntrain; ++i) {
+            const double w = ht[4 * (size_t)perm[i] + 3];
+            sw += w * w;
+        }
+        wnorm = sw > 0.0 ? (float)((double)ntrain / sw) : 0.f;
+    }
     int* d_perm = nullptr;
     NBG_CUDA(e, cudaMalloc(&d_perm, total * sizeof(int)));
     NBG_CUDA(e, cudaMemcpyAsync(d_perm, perm.data(), total * sizeof(int), cudaMemcpyHostToDevice,
@@ -1099,7 +1120,7 @@ nbg_status nbg_learn_train(nbg_engine* e, int epochs, size_t batch, double lr, u
         NBG_CUDA(e, cudaMemsetAsync(L->loss, 0, 2 * sizeof(double), e->stream));
         for (size_t b0 = 0; b0 < ntrain; b0 += batch, ++step) {
             const size_t bs = std::min(batch, ntrain - b0);
-            nbg_status s = run_train_pass(e, L->x, L->t, d_perm, b0, bs);
+            nbg_status s = run_train_pass(e, L->x, L->t, d_perm, b0, bs, wnorm);
             if (s != NBG_OK) return s;
             // cosine-decayed learning rate
             const double frac = total_steps > 1 ? (double)step / (double)(total_steps - 1) : 0.0;
@@ -1123,7 +1144,7 @@ nbg_status nbg_learn_train(nbg_engine* e, int epochs, size_t batch, double lr, u
     double val = 0.0;
     if (nval > 0) {
         NBG_CUDA(e, cudaMemsetAsync(L->loss, 0, 2 * sizeof(double), e->stream));
-        nbg_status s = run_train_pass(e, L->x, L->t, d_perm, ntrain, nval);
+        nbg_status s = run_train_pass(e, L->x, L->t, d_perm, ntrain, nval, wnorm);
         if (s != NBG_OK) return s;
         NBG_CUDA(e, cudaMemsetAsync(L->grad, 0, kParams * sizeof(float), e->stream));
         double h[2] = {0, 0};
