@@ -186,9 +186,13 @@ nbg_status nbg_bh_stack_peak(nbg_engine* e, uint64_t* peak, uint64_t* capacity);
  * for a body-cell interaction accepted at the engine's ratio lambda_l but
  * inside the band lambda_l < lambda <= learned_tight_ratio, the residual
  * between the cell's exact subtree acceleration and its monopole, in units
- * of m / s^2 (s = cell radius).  Used when nbg_params.learned = 1 (Barnes-Hut,
- * mixed precision); tuning key "learned.group" selects one sample per
- * (body, cell) (0, default) or per (warp, cell) at the warp centroid (1). */
+ * of m / s^2 (s = cell radius).  Its three outputs c weight the vectors
+ * u/|u|, Q u/|u| and the mass-centre offset o of the features (g = c0 u/|u|
+ * + c1 Q u/|u| + c2 o); nbg_learn_predict returns c.  Used when
+ * nbg_params.learned = 1 (Barnes-Hut, mixed precision); tuning keys:
+ * "learned.group" one sample per (body, cell) (0, default) or per (warp,
+ * cell) at the warp centroid (1); "learned.weighted" (0 default, 1: training
+ * loss weighted by the cell's force scale (m / s^2)^2). */
 size_t nbg_learn_param_count(void);
 nbg_status nbg_learn_set_weights(nbg_engine* e, const float* w, size_t count);
 nbg_status nbg_learn_get_weights(nbg_engine* e, float* w, size_t count);
