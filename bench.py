@@ -232,14 +232,15 @@ def read_traffic():
 
 
 def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 5, walk: int = 1,
-             weights=None, order: int = 1):
+             weights=None, order: int = 1, build_rate: int = 0):
     """Barnes-Hut fcompute (tree rebuilt every call) at opening ratio lam.
     walk 1 = group walk with interaction lists, 0 = warp-coherent stackless."""
     from nbody_gb300 import _lib
     from nbody_gb300.engine import create_engine
     e = create_engine({"engine": "gb300", "algo": "bh", "precision": "mixed",
                        "softening": SOFTENING, "distance_to_node_radius_ratio": lam,
-                       "learned": learned, "tree_layout": "heap_stackless"})
+                       "learned": learned, "tree_layout": "heap_stackless",
+                       "tree_build_rate": build_rate})
     if e is None:
         return {"unavailable": "engine not created"}
     e.tune_set("bh.walk", walk)
@@ -249,14 +250,19 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
     if weights is not None:
         e.learn_set_weights(weights)
     f = e.create_buffer(8 * 6 * n_bh)
+    step = 0
     for _ in range(2):
+        e.set_step(step)
         e.fcompute(0.0, e.get_y(), f)
+        step += 1
     e.synchronize()
     e.bh_counters()
     e.profile_enable(True)
     t0 = time.perf_counter()
     for _ in range(calls):
+        e.set_step(step)  # with build_rate > 0: a full build every build_rate steps, refits between
         e.fcompute(0.0, e.get_y(), f)
+        step += 1
     e.synchronize()
     wall = (time.perf_counter() - t0) / calls
     tb, nb = e.profile_query(_lib.K_TREE_BUILD)
@@ -267,7 +273,7 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
     a = out[3 * n_bh:].reshape(3, n_bh).T[rows]
     rel = np.linalg.norm(a - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
     e.close()
-    ms = (tb / max(nb, 1) + tw / max(nw, 1))
+    ms = (tb + tw) / calls
     # node records read by the walk (20 B each: com.xyz + crit^2, mass), per
     # warp test, plus the body rows (16 B in, 24 B out)
     walk_bytes = visits / calls * 20.0 + n_bh * 40.0
@@ -275,7 +281,7 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
             "bodies_per_s": n_bh / (ms * 1e-3),
             "walk_node_gbs": walk_bytes / (tw / max(nw, 1) * 1e-3) / 1e9,
             "ms_per_fcompute": ms, "wall_ms_per_fcompute": wall * 1e3,
-            "build_ms": tb / max(nb, 1), "walk_ms": tw / max(nw, 1),
+            "build_ms": tb / calls, "walk_ms": tw / max(nw, 1),
             "p50": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99)),
             "interactions_per_body": inter / calls / n_bh,
             "warp_node_visits_per_warp": visits / calls / (n_bh / 32)}
@@ -396,6 +402,10 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20):
     res["quadrupole_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, order=2)
     res["quadrupole_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d, order=2)
     res["coherent_walk_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, walk=0)
+    # tree_build_rate 4 (the reference's refit option): one build and three
+    # refits per four fcomputes; same positions, so the same forces
+    res["refit_rate4_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, calls=8,
+                                            build_rate=4)
     w, fit = train_correction()
     res["learned_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=w)
     res["learned_theta_0.9"]["training"] = fit
@@ -406,6 +416,35 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20):
         "bodies_per_s_ratio": l09["bodies_per_s"] / p05["bodies_per_s"],
         "p99_ratio": l09["p99"] / p05["p99"]}
     return res
+
+
+def run_stats_bench(n: int = N_BODIES):
+    """P, L, E, V of one state: the GPU's FP64 reductions
+    against the reference's single-threaded host sums (nbody/nbody_data.cpp:
+    57-145, restated in the oracle) timed on a 16384-body sample and scaled
+    by the O(N^2) potential term."""
+    from nbody_gb300.data import NBodyData
+    from nbody_gb300.engine import create_engine
+    from oracle.oracle import load_oracle
+    d = NBodyData.plummer(n, seed=1)
+    e = create_engine({"engine": "gb300", "precision": "mixed", "softening": SOFTENING})
+    e.init(d)
+    e.statistics()
+    e.synchronize()
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        e.statistics()
+    gpu_ms = (time.perf_counter() - t0) / reps * 1e3
+    e.close()
+    m = 16384
+    sub = NBodyData.plummer(m, seed=1)
+    orc = load_oracle()
+    t0 = time.perf_counter()
+    orc.statistics(sub.to_state(), sub.mass)
+    cpu_ms = (time.perf_counter() - t0) * 1e3 * (n / m) ** 2
+    return {"n": n, "gpu_ms": gpu_ms, "cpu_single_thread_ms_scaled": cpu_ms,
+            "cpu_sample": f"{m} bodies, scaled by (N / {m})^2"}
 
 
 def run_ensemble_suite(steps: int = 20):
@@ -564,6 +603,7 @@ def run_gb300(args):
 
     bh = run_bh_suite(rank, args.bh_n) if (rank == 0 and not args.no_bh) else None
     ensemble = run_ensemble_suite() if (rank == 0 and not args.no_ensemble) else None
+    stats = run_stats_bench(n) if (rank == 0 and not args.no_ensemble) else None
 
     if rank == 0:
         line = {
@@ -597,6 +637,7 @@ def run_gb300(args):
             "clocks": clk,
             "force_error": err,
             "bh": bh,
+            "statistics": stats,
             "ensemble": ensemble,
             "wall_s_timed": wall,
         }

@@ -85,8 +85,23 @@ struct PairUnit {
     int i0;  // first body (system-local) of the 256-body block
 };
 
+// 1 / sqrt(x) in FP64: the FP32 hardware estimate (about 23 correct bits)
+// refined by two Newton-Raphson steps y <- y (3 - x y^2) / 2 (each doubles
+// the correct bits), so the result is within a few ulp of the correctly
+// rounded value; outside the FP32 range the division form is used.
+__device__ __forceinline__ double rsqrt_fp64(double x) {
+    if (!(x > 1e-30 && x < 1e30)) return 1.0 / sqrt(x);
+    double y = (double)rsqrtf((float)x);
+    const double h = 0.5 * x;
+    y = y * fma(-h * y, y, 1.5);
+    y = y * fma(-h * y, y, 1.5);
+    return y;
+}
+
 // Potential energy: one CTA per (system, 256 i-bodies); FP64 pair sums over
-// j-tiles in shared memory; one atomicAdd per CTA into PE[s] (pre-halved).
+// j-tiles in shared memory, each unordered pair once (j tiles from the
+// CTA's own on; pairs in later tiles count twice, the potential being
+// symmetric); one atomicAdd per CTA into PE[s] (pre-halved).
 __global__ void __launch_bounds__(kStatThreads)
 stats_potential_kernel(const double* __restrict__ y, const double* __restrict__ mass, size_t stride,
                        const long long* __restrict__ off, const int* __restrict__ cnt,
@@ -102,7 +117,7 @@ stats_potential_kernel(const double* __restrict__ y, const double* __restrict__ 
     const size_t i = (size_t)(o + (live ? li : 0));
     const double xi = y[i], yi = y[stride + i], zi = y[2 * stride + i], mi = live ? mass[i] : 0.0;
     double pe = 0.0;
-    for (int j0 = 0; j0 < n; j0 += kStatThreads) {
+    for (int j0 = u.i0; j0 < n; j0 += kStatThreads) {
         const int lj = j0 + threadIdx.x;
         __syncthreads();
         if (lj < n) {
@@ -114,13 +129,16 @@ stats_potential_kernel(const double* __restrict__ y, const double* __restrict__ 
         }
         __syncthreads();
         const int c = min(kStatThreads, n - j0);
+        const bool own = j0 == u.i0;
+        double tile = 0.0;
         for (int k = 0; k < c; ++k) {
-            if (j0 + k == li) continue;
+            if (own && j0 + k == li) continue;
             const double dx = xi - tx[k], dy = yi - ty[k], dz = zi - tz[k];
             const double r2 = dx * dx + dy * dy + dz * dz;
             if (eps2 == 0.0 && r2 < kMinDistance) continue;
-            pe -= tm[k] / sqrt(r2 + eps2);
+            tile -= tm[k] * rsqrt_fp64(r2 + eps2);
         }
+        pe += own ? tile : 2.0 * tile;
     }
     const double tot = block_sum(pe * mi, sh);
     if (threadIdx.x == 0) atomicAdd(out + 12 * (size_t)u.sys + 7, tot / 2);
