@@ -553,8 +553,12 @@ def run_gb300(args):
     e.profile_enable(False)
     k_avg_s = kms / max(klaunch, 1) * 1e-3
     achieved_tflops = n * n * FLOP_PER_PAIR / k_avg_s / 1e12
-    n_pad = -(-n // 1024) * 1024
-    pairs_evaluated = n_pad * (n_pad + 1024) // 2
+    if int(tuning["best"].get("direct.symmetric", 1)) != 0:
+        rng_sz = 256 * int(tuning["best"].get("direct.sym_g", 4))  # bodies per symmetric range
+        n_pad = -(-n // rng_sz) * rng_sz
+        pairs_evaluated = n_pad * (n_pad + rng_sz) // 2
+    else:
+        pairs_evaluated = n * n
     peak_flops = e.measure_fp32_peak()
     props = torch.cuda.get_device_properties(local)
     nominal = props.multi_processor_count * 128 * 2 * 2.07e9

@@ -231,6 +231,8 @@ uint64_t nbg_launch_count(const nbg_engine* e);
 /* Tuning knobs (set by the autotuner or by hand; no reference counterpart).
  * Keys: "direct.symmetric" (1: each unordered pair evaluated once and
  *       applied to both bodies, the default; 0: one-sided kernel),
+ *       "direct.sym_g" (4 or 3: packed A-body pairs per lane of the
+ *       symmetric kernel; 3 runs 5 CTAs per SM),
  *       "direct.sym_blocks" (4 or 5: CTAs per SM the symmetric kernel's
  *       register budget is set for), "direct.sym_unroll" (1, 2 or 4: unroll
  *       of its 32-step rotation loop, default 4),

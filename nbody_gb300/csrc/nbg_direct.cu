@@ -320,8 +320,9 @@ MixedKernel pick_mixed(int G, int unr) {
 // ---------------------------------------------------------------------------
 // symmetric mixed kernel: every unordered pair evaluated once
 // ---------------------------------------------------------------------------
-// Bodies are split into ranges of kSymRange.  A CTA holds one range in
-// registers (the A bodies: 8 per lane, as 4 packed FP32x2 pairs) and streams
+// Bodies are split into ranges of 256 G bodies.  A CTA holds one range in
+// registers (the A bodies: 2 G per lane as G packed FP32x2 pairs, G = 4 by
+// default, 3 with 5 CTAs per SM) and streams
 // 128-body B tiles through the same TMA ring as above.  Unit (R, t) pairs
 // range R with tile t for t >= the first tile of R:
 //   * t inside R: one-sided, all ordered pairs, A side only (the self pair
@@ -330,7 +331,7 @@ MixedKernel pick_mixed(int G, int unr) {
 //     -m_A d / r^3 to B (Newton's third law), so tiles before R are covered
 //     by the units of their own ranges.
 // Symmetric chunks of 32 B bodies rotate through the warp: at step k lane l
-// meets B body (l + k) mod 32 with its 8 A bodies, and the B accumulator
+// meets B body (l + k) mod 32 with its 2 G A bodies, and the B accumulator
 // follows its body one lane down per step (a shuffle), so after 32 steps lane
 // l holds the complete warp sum for B body l and adds it to f with FP64
 // reductions.  Per pair this costs 16 FP32 operations and one reciprocal
@@ -338,10 +339,10 @@ MixedKernel pick_mixed(int G, int unr) {
 // the one-sided kernel.
 constexpr int kSymWarps = 4;
 constexpr int kSymThreads = kSymWarps * 32;
-constexpr int kSymG = 4;
-constexpr int kSymRange = kSymThreads * 2 * kSymG;  // 1024 A bodies per range
-constexpr int kSymT = 128;                            // B bodies per tile
-constexpr int kSymTilesPerRange = kSymRange / kSymT;  // 8
+constexpr int kSymT = 128;  // B bodies per tile
+// G packed pairs of A bodies per lane (4 by default, 3 with "direct.sym_g");
+// a range is 256 G bodies, 2 G tiles
+__host__ __device__ constexpr int sym_range(int G) { return kSymThreads * 2 * G; }
 constexpr int kSymStages = 4;
 constexpr uint32_t kSymTileBytes = kSymT * 32;  // (x x y y | z z m m) FP32 per body
 
@@ -350,7 +351,7 @@ struct SymArgs {
     double* acc;           // a-part of f: [3][n]
     int n;
     int n_jt;              // tiles = n_pad / kSymT
-    int n_ranges;          // n_pad / kSymRange
+    int n_ranges;          // n_pad / range
     long long units;
     float eps2;
     unsigned* err;
@@ -385,27 +386,29 @@ __global__ void pack_sym_kernel(const double* __restrict__ y, const double* __re
     }
 }
 
-// First unit of range R: sum over R' < R of (n_jt - 8 R').
-__device__ __forceinline__ long long sym_range_start(long long R, long long n_jt) {
-    return R * n_jt - (long long)kSymTilesPerRange * (R * (R - 1) / 2);
+// First unit of range R: sum over R' < R of (n_jt - tpr R'), tpr = tiles per range.
+__host__ __device__ __forceinline__ long long sym_range_start(long long R, long long n_jt,
+                                                              int tpr) {
+    return R * n_jt - (long long)tpr * (R * (R - 1) / 2);
 }
 
+template <int TPR>
 struct SymCursor {
     int R, t;
     __device__ void locate(long long u, int n_jt, int n_ranges) {
         int lo = 0, hi = n_ranges - 1;  // largest R with start(R) <= u
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (sym_range_start(mid, n_jt) <= u) lo = mid;
+            if (sym_range_start(mid, n_jt, TPR) <= u) lo = mid;
             else hi = mid - 1;
         }
         R = lo;
-        t = (int)(u - sym_range_start(lo, n_jt)) + kSymTilesPerRange * lo;
+        t = (int)(u - sym_range_start(lo, n_jt, TPR)) + TPR * lo;
     }
     __device__ void next(int n_jt) {
         if (++t == n_jt) {
             ++R;
-            t = kSymTilesPerRange * R;
+            t = TPR * R;
         }
     }
 };
@@ -444,10 +447,11 @@ __device__ __forceinline__ void sym_issue(float4* tiles, uint64_t* full, int s, 
     bulk_g2s(tiles + s * 2 * kSymT, bodies + (size_t)t * 2 * kSymT, kSymTileBytes, &full[s]);
 }
 
-template <bool CLAMP, int MINB, int RUNR>
+template <bool CLAMP, int MINB, int RUNR, int G = 4>
 __global__ void __launch_bounds__(kSymThreads, MINB)
 direct_sym_kernel(SymArgs a) {
-    constexpr int G = kSymG;
+    constexpr int kSymRange = sym_range(G);
+    constexpr int kSymTilesPerRange = kSymRange / kSymT;
     constexpr int kSlots = 6 * G;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float4* tiles = reinterpret_cast<float4*>(smem_raw);
@@ -472,7 +476,7 @@ direct_sym_kernel(SymArgs a) {
         mbar_fence_init();
     }
     __syncthreads();
-    SymCursor cons, prod;
+    SymCursor<kSymTilesPerRange> cons, prod;
     cons.locate(u0, a.n_jt, a.n_ranges);
     prod = cons;
     if (producer) {
@@ -612,15 +616,17 @@ direct_sym_kernel(SymArgs a) {
     if (ok && cur_R >= 0) flush(cur_R);
 }
 
-size_t sym_smem_bytes() {
+size_t sym_smem_bytes(int G) {
     return (size_t)kSymStages * kSymTileBytes + 2 * kSymStages * sizeof(uint64_t) +
-           6 * kSymG * kSymThreads * sizeof(f2_t);
+           6 * G * kSymThreads * sizeof(f2_t);
 }
 
 nbg_status direct_sym_launch(nbg_engine* e, const double* y, double* f) {
     const int n = (int)e->count;
-    const int n_ranges = (n + kSymRange - 1) / kSymRange;
-    const int n_pad = n_ranges * kSymRange;
+    const int G = e->tune_get("direct.sym_g", 4) == 3 ? 3 : 4;
+    const int range = sym_range(G);
+    const int n_ranges = (n + range - 1) / range;
+    const int n_pad = n_ranges * range;
     const size_t need = 2 * (size_t)n_pad * sizeof(float4);
     if (e->xyzm_cap < need) {
         cudaFree(e->d_xyzm);
@@ -641,7 +647,9 @@ nbg_status direct_sym_launch(nbg_engine* e, const double* y, double* f) {
     const int64_t ru = e->tune_get("direct.sym_unroll", 4);
     using SymKernel = void (*)(SymArgs);
     SymKernel kern;
-    if (b5)
+    if (G == 3)  // 6 A bodies per lane: fewer registers, 5 CTAs per SM
+        kern = clamp ? direct_sym_kernel<true, 5, 4, 3> : direct_sym_kernel<false, 5, 4, 3>;
+    else if (b5)
         kern = clamp ? direct_sym_kernel<true, 5, 2> : direct_sym_kernel<false, 5, 2>;
     else if (ru >= 4)
         kern = clamp ? direct_sym_kernel<true, 4, 4> : direct_sym_kernel<false, 4, 4>;
@@ -649,7 +657,7 @@ nbg_status direct_sym_launch(nbg_engine* e, const double* y, double* f) {
         kern = clamp ? direct_sym_kernel<true, 4, 1> : direct_sym_kernel<false, 4, 1>;
     else
         kern = clamp ? direct_sym_kernel<true, 4, 2> : direct_sym_kernel<false, 4, 2>;
-    const size_t smem = sym_smem_bytes();
+    const size_t smem = sym_smem_bytes(G);
     NBG_CUDA(e, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));
     int occ = 0;
@@ -663,8 +671,7 @@ nbg_status direct_sym_launch(nbg_engine* e, const double* y, double* f) {
     a.n = n;
     a.n_jt = n_pad / kSymT;
     a.n_ranges = n_ranges;
-    a.units = (long long)n_ranges * a.n_jt -
-              (long long)kSymTilesPerRange * ((long long)n_ranges * (n_ranges - 1) / 2);
+    a.units = sym_range_start(n_ranges, a.n_jt, range / kSymT);
     a.eps2 = (float)(e->params.softening * e->params.softening);
     a.err = e->d_err;
     long long grid = (long long)e->sm_count * occ;

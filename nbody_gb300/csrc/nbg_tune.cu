@@ -58,6 +58,7 @@ std::vector<Candidate> direct_candidates() {
     for (int ru : {1, 2})
         c.push_back({{"direct.symmetric", 1}, {"direct.sym_blocks", 4}, {"direct.sym_unroll", ru},
                      {"direct.blocks_per_sm", 0}});
+    c.push_back({{"direct.symmetric", 1}, {"direct.sym_g", 3}, {"direct.blocks_per_sm", 0}});
     for (int g : {4, 2})
         for (int unr : {2, 4, 8}) {
             if (g == 4 && unr == 8) continue;  // not instantiated

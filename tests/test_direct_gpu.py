@@ -103,7 +103,7 @@ def test_mixed_plummer_force_error(make_engine, oracle, sym):
 
 
 @pytest.mark.parametrize("n", [1, 2, 15, 63, 65, 127, 129, 513, 1000, 1025, 2047, 5000])
-@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed-onesided"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed-onesided", "mixed-g3"])
 def test_ragged_sizes(make_engine, oracle, n, prec):
     """Sizes around the tile (128) and range (1024) boundaries; above 1024
     bodies the symmetric kernel has pairs of ranges."""
@@ -111,6 +111,8 @@ def test_ragged_sizes(make_engine, oracle, n, prec):
     e = make_engine(precision=prec.split("-")[0])
     if prec == "mixed-onesided":
         e.tune_set("direct.symmetric", 0)
+    if prec == "mixed-g3":  # symmetric kernel with 768-body ranges
+        e.tune_set("direct.sym_g", 3)
     assert e.init(d)
     y = d.to_state()
     f = _f_gpu(e, y)
@@ -125,12 +127,14 @@ def test_ragged_sizes(make_engine, oracle, n, prec):
         assert np.all(f[3:] == 0.0)
 
 
-@pytest.mark.parametrize("sym", [0, 1])
+@pytest.mark.parametrize("sym", [0, 1, 3])
 def test_full_size_sampled_and_momentum(make_engine, oracle, sym):
     n = 131072
     d = NBodyData.plummer(n, seed=11)
     e = make_engine(precision="mixed", softening=1e-3)
-    e.tune_set("direct.symmetric", sym)
+    e.tune_set("direct.symmetric", min(sym, 1))
+    if sym == 3:
+        e.tune_set("direct.sym_g", 3)
     assert e.init(d)
     y = d.to_state()
     f = _f_gpu(e, y)
