@@ -232,9 +232,10 @@ def read_traffic():
 
 
 def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 5, walk: int = 1,
-             weights=None, order: int = 1, build_rate: int = 0):
+             weights=None, order: int = 1, build_rate: int = 0, build: int = 2):
     """Barnes-Hut fcompute (tree rebuilt every call) at opening ratio lam.
-    walk 1 = group walk with interaction lists, 0 = warp-coherent stackless."""
+    walk 1 = group walk with interaction lists, 0 = warp-coherent stackless;
+    build 0 = the reference's kd-median tree, 1 Morton, 2 Hilbert order."""
     from nbody_gb300 import _lib
     from nbody_gb300.engine import create_engine
     e = create_engine({"engine": "gb300", "algo": "bh", "precision": "mixed",
@@ -245,6 +246,7 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
         return {"unavailable": "engine not created"}
     e.tune_set("bh.walk", walk)
     e.tune_set("bh.order", order)
+    e.tune_set("bh.build", build)
     if not e.init(d):
         return {"unavailable": "engine init failed"}
     if weights is not None:
@@ -278,6 +280,7 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
     # warp test, plus the body rows (16 B in, 24 B out)
     walk_bytes = visits / calls * 20.0 + n_bh * 40.0
     return {"lambda": lam, "theta": 1.0 / lam, "walk": walk, "learned": learned, "order": order,
+            "build": ("kd-median", "morton", "hilbert")[build],
             "bodies_per_s": n_bh / (ms * 1e-3),
             "walk_node_gbs": walk_bytes / (tw / max(nw, 1) * 1e-3) / 1e9,
             "ms_per_fcompute": ms, "wall_ms_per_fcompute": wall * 1e3,
@@ -288,7 +291,7 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
 
 
 def bh_rkdp_run(n_bh: int, d, advises: int = 5, dt: float = 1e-3):
-    """SURVEY config 3 as the reference would run it: the rkdp solver
+    """The 2^20-body Barnes-Hut run as the reference would drive it: the rkdp solver
     (nbody/nbody_solver_rk_butcher.cpp, error threshold 1e-6 on the unscaled
     max |sum (b2 - b1) k|) driving the Barnes-Hut engine (theta 0.5, tree
     rebuilt every fcompute) for `advises` advise calls.  The embedded error of
@@ -333,10 +336,12 @@ def accuracy_target(n_bh: int, rows, a_ref, d, target: float = 1e-4):
     error falls slowly in the tail) and the direct sum."""
     from nbody_gb300.engine import create_engine
     cands = []
-    for order, lams in ((2, (3.0, 3.5, 4.0, 6.0, 8.0)), (1, (16.0, 32.0, 48.0))):
+    for build, order, lams in ((2, 2, (4.0, 4.5, 5.0, 6.0, 8.0)), (0, 2, (3.0, 3.5, 4.0, 6.0, 8.0)),
+                               (2, 1, (16.0, 32.0, 48.0))):
         for lam in lams:
-            r = bench_bh(n_bh, lam, False, rows, a_ref, d, calls=2, order=order)
-            cands.append({"path": f"bh {'quadrupole' if order == 2 else 'monopole'} lambda={lam:g}",
+            r = bench_bh(n_bh, lam, False, rows, a_ref, d, calls=3, order=order, build=build)
+            cands.append({"path": f"bh {r['build']} {'quadrupole' if order == 2 else 'monopole'} "
+                                  f"lambda={lam:g}",
                           "ms": r["ms_per_fcompute"], "p99": r["p99"], "p50": r["p50"]})
             if r["p99"] <= target:
                 break
@@ -397,17 +402,27 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20):
     res = {"workload": f"Barnes-Hut fcompute, N={n_bh} Plummer, softening 1e-3, heap_stackless, "
                        "tree rebuilt every call, FP32 walk / FP64 state",
            "error_judge": "FP64 direct sum (oracle) on 4096 sampled bodies"}
-    res["plain_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d)
-    res["plain_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d)
-    res["quadrupole_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, order=2)
-    res["quadrupole_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d, order=2)
-    res["coherent_walk_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, walk=0)
+    # the reference's kd-median tree at the reference's opening ratios, then
+    # the default Hilbert tree at the same ratios and at lambda 2.5, where
+    # both its p50 and p99 are below the kd tree's at theta 0.5
+    res["plain_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, build=0)
+    res["plain_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d, build=0)
+    res["hilbert_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d)
+    res["hilbert_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d)
+    res["hilbert_lambda_2.5"] = bench_bh(n_bh, 2.5, False, rows, a_ref, d)
+    res["morton_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, build=1)
+    res["quadrupole_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, order=2, build=0)
+    res["quadrupole_hilbert_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, order=2)
+    res["coherent_walk_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, walk=0, build=0)
     # tree_build_rate 4 (the reference's refit option): one build and three
     # refits per four fcomputes; same positions, so the same forces
     res["refit_rate4_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, calls=8,
-                                            build_rate=4)
+                                            build_rate=4, build=0)
+    res["refit_rate4_hilbert_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, calls=8,
+                                                    build_rate=4)
     w, fit = train_correction()
-    res["learned_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=w)
+    res["learned_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=w,
+                                        build=0)
     res["learned_theta_0.9"]["training"] = fit
     res["accuracy_target_1e-4"] = accuracy_target(n_bh, rows, a_ref, d)
     res["rkdp_theta_0.5"] = bh_rkdp_run(n_bh, d)
@@ -419,7 +434,7 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20):
 
 
 def run_stats_bench(n: int = N_BODIES):
-    """P, L, E, V of one state: the GPU's FP64 reductions
+    """P, L, E, V of one state (the run's conservation check): the GPU's FP64 reductions
     against the reference's single-threaded host sums (nbody/nbody_data.cpp:
     57-145, restated in the oracle) timed on a 16384-body sample and scaled
     by the O(N^2) potential term."""

@@ -181,6 +181,11 @@ nbg_status nbg_bh_counters(nbg_engine* e, uint64_t* visits, uint64_t* interactio
  * current tree (48 entries per level + 32); a walk that would exceed the
  * capacity stops and reports NBG_ERR_DEVICE_ERROR. */
 nbg_status nbg_bh_stack_peak(nbg_engine* e, uint64_t* peak, uint64_t* capacity);
+/* Groups the group walk handed to the per-body fallback walk since the last
+ * nbg_bh_counters call: a group walk gives up after "bh.test_cap" node tests
+ * (default max(N / 4, 2^16)), which only groups spread over much of the
+ * system reach, and its bodies are walked one by one. */
+nbg_status nbg_bh_fallback_groups(nbg_engine* e, uint64_t* groups);
 /* ---- learned monopole correction (no reference counterpart) ----
  * A 16 -> 64 -> 64 -> 3 GELU MLP (BF16 weights, FP32 accumulate) predicts,
  * for a body-cell interaction accepted at the engine's ratio lambda_l but
@@ -242,6 +247,13 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       "bh.walk" (1: group walk with interaction lists, 0: warp-coherent
  *       stackless walk) for the mixed-precision Barnes-Hut path,
  *       "bh.group" (64 or 32 bodies per warp in the group walk),
+ *       "bh.build" (0: the reference's kd-median tree, always for FP64;
+ *       mixed precision: 1 leaves in Morton order, 2 in Hilbert order (the
+ *       default without the learned correction), every node the two halves of its range -- one sort
+ *       instead of three, a different tree with compact cells),
+ *       "bh.test_cap" (node tests after which a group walk hands its bodies
+ *       to the per-body walk; 0, the default, is "bh.test_cap_ratio"
+ *       (default 3) times the previous walk's mean per group),
  *       "bh.order" (1: monopole cells as the reference; 2: accepted cells
  *       add their quadrupole term, from FP32 second moments per node),
  *       "bh.walk_blocks" (4, 5, 6 or 8: CTAs per SM the group walk's register

@@ -44,7 +44,7 @@ EXPORTS = [
     "nbg_ensemble_launch_count", "nbg_ensemble_profile", "nbg_autotune",
     "nbg_ensemble_autotune", "nbg_stream_open", "nbg_stream_set_header", "nbg_stream_write",
     "nbg_stream_write_host", "nbg_stream_flush", "nbg_stream_close", "nbg_stream_last_error",
-    "nbg_bh_stack_peak",
+    "nbg_bh_stack_peak", "nbg_bh_fallback_groups",
 ]
 
 
@@ -146,6 +146,7 @@ def load() -> C.CDLL:
     _proto(lib, "nbg_direct_mixed_noalloc", i32, vp, vp, vp, sz, dbl, vp)
     _proto(lib, "nbg_bh_counters", i32, vp, C.POINTER(u64), C.POINTER(u64))
     _proto(lib, "nbg_bh_stack_peak", i32, vp, C.POINTER(u64), C.POINTER(u64))
+    _proto(lib, "nbg_bh_fallback_groups", i32, vp, C.POINTER(u64))
     fp = C.POINTER(C.c_float)
     ip = C.POINTER(C.c_int)
     _proto(lib, "nbg_learn_param_count", sz)

@@ -24,6 +24,8 @@
 //    nodes at a time against the bounding box of its 32 bodies and evaluates
 //    the accepted nodes from an interaction list in shared memory with packed
 //    FP32x2 pair math (details at bh_group_walk_kernel).
+#include <algorithm>
+
 #include "nbg_ptx.cuh"
 #include "nbg_tree.cuh"
 
@@ -192,6 +194,9 @@ struct GroupSmem {  // followed by the stacks, kGWWarps x stack_cap ints
 
 inline int group_stack_cap(int levels) { return kGWStackPerLevel * (levels + 1) + 32; }
 
+// groups whose node tests set the group walk's test cap
+constexpr int kCapSamples = 256;
+
 // Second list of the quadrupole walk (bh.order = 2): accepted cells with their
 // second moments; leaves stay in the monopole list.  Arrays in the order
 // x, y, z, m, Mxx, Myy, Mzz, tr M / 2, Mxy, Mxz, Myz.
@@ -327,7 +332,8 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
     if (lane == 0) stack[0] = 0;
     __syncwarp();
     int sp = 1, lc = 0, peak = 1;
-    bool overflow = false;
+    bool overflow = false, abandoned = false;
+    const unsigned long long test_cap = t.test_cap != 0 ? t.test_cap : t.cap_state[0];
 
     auto evaluate = [&]() {
         // pad to a whole quad with massless entries
@@ -444,6 +450,10 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
             }
         }
         tests += (unsigned long long)__popc(__ballot_sync(0xffffffffu, valid));
+        if (tests > test_cap) {  // a group spread over much of the system:
+            abandoned = true;      // its bodies are walked one by one instead
+            break;
+        }
         // cells with moments go to the quadrupole list (ORDER 2), the rest
         // (leaves, or every node for ORDER 1) to the monopole list
         const bool to_quad = ORDER == 2 && accept && c < n;
@@ -491,6 +501,17 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
     if (overflow) {
         if (lane == 0) atomicOr(err, kDevErrWalkOverflow);
     }
+    if (lane == 0) {
+        atomicAdd(&t.counters[0], tests);
+        atomicMax(&t.counters[2], (unsigned long long)peak);
+    }
+    if (abandoned) {
+        if (lane == 0) {
+            t.fb_list[atomicAdd(t.fb_count, 1u)] = gw;
+            atomicAdd(&t.counters[3], 1ull);
+        }
+        return;
+    }
     if (lc > 0) evaluate();
     if (ORDER == 2 && qc > 0) evaluate_quad();
 #pragma unroll
@@ -510,10 +531,161 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
         f2_unpack(slot(6 * bb + 5), l0, l1);
         f[5 * n + b] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
     }
-    if (lane == 0) {
-        atomicAdd(&t.counters[0], tests);
-        atomicAdd(&t.counters[1], inter * 32ull * BPL);
-        atomicMax(&t.counters[2], (unsigned long long)peak);
+    if (lane == 0) atomicAdd(&t.counters[1], inter * 32ull * BPL);
+}
+
+// Node tests of a sample of groups (every stride-th), counted by the group
+// walk's own traversal without its force evaluation; a sample stops
+// counting past `limit`.  Their median times a ratio is the walk's test
+// cap, a function of this tree alone, so that equal trees give equal forces.
+template <int BPL>
+__global__ void __launch_bounds__(kGWThreads)
+bh_group_count_kernel(int n, int stride, int samples, TreeState t, int stack_cap,
+                      unsigned long long limit) {
+    extern __shared__ int count_stacks[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int smp = blockIdx.x * kGWWarps + warp;
+    if (smp >= samples) return;
+    const int gw = smp * stride;
+    float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+#pragma unroll
+    for (int b = 0; b < BPL; ++b) {
+        const float4 me = __ldg(&t.node4[n + gw * 32 * BPL + b * 32 + lane]);
+        lo[0] = fminf(lo[0], me.x);
+        lo[1] = fminf(lo[1], me.y);
+        lo[2] = fminf(lo[2], me.z);
+        hi[0] = fmaxf(hi[0], me.x);
+        hi[1] = fmaxf(hi[1], me.y);
+        hi[2] = fmaxf(hi[2], me.z);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+    int* stack = count_stacks + warp * stack_cap;
+    const unsigned lt = (1u << lane) - 1u;
+    if (lane == 0) stack[0] = 0;
+    __syncwarp();
+    int sp = 1;
+    unsigned long long tests = 0;
+    while (sp > 0 && tests <= limit) {
+        const int k = min(sp, 16);
+        int c = 0;
+        if (lane < 2 * k) c = 2 * stack[sp - 1 - (lane >> 1)] + (lane & 1);
+        __syncwarp();
+        sp -= k;
+        const bool valid = lane < 2 * k && c != 0;
+        bool open = false;
+        if (valid && c < n) {
+            const float4 nd = __ldg(&t.node4[c]);
+            const float ex = fmaxf(fmaxf(lo[0] - nd.x, nd.x - hi[0]), 0.f);
+            const float ey = fmaxf(fmaxf(lo[1] - nd.y, nd.y - hi[1]), 0.f);
+            const float ez = fmaxf(fmaxf(lo[2] - nd.z, nd.z - hi[2]), 0.f);
+            open = !(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > nd.w);
+        }
+        tests += (unsigned long long)__popc(__ballot_sync(0xffffffffu, valid));
+        const unsigned om = __ballot_sync(0xffffffffu, open);
+        const int npush = __popc(om);
+        if (sp + npush > stack_cap) break;  // the walk itself reports an overflow
+        if (open) stack[sp + __popc(om & lt)] = c;
+        sp += npush;
+        __syncwarp();
+    }
+    if (lane == 0) t.cap_state[1 + smp] = tests;
+}
+
+// The test cap: ratio x the median of the sampled counts (at least 4096).
+// One block of `samples` threads; each finds its value's rank.
+__global__ void bh_test_cap_kernel(TreeState t, int samples, unsigned ratio) {
+    const int i = threadIdx.x;
+    if (i >= samples) return;
+    const unsigned long long v = t.cap_state[1 + i];
+    int rank = 0;
+    for (int j = 0; j < samples; ++j) {
+        const unsigned long long u = t.cap_state[1 + j];
+        rank += (u < v || (u == v && j < i)) ? 1 : 0;
+    }
+    if (rank == samples / 2) t.cap_state[0] = max((unsigned long long)ratio * v, 4096ull);
+}
+
+// The bodies of the groups the group walk gave up on: one lane per body,
+// the reference's per-body stackless walk (accept when d^2 > crit^2, then
+// skip the subtree; leaves have crit^2 = 0, so a body skips itself), FP32
+// records, two-sum accumulation, the quadrupole term with ORDER 2 as in the
+// group walk.
+template <bool CLAMP, int BPL, int ORDER>
+__global__ void __launch_bounds__(128)
+bh_body_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n, float eps2,
+                    TreeState t, unsigned* err) {
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    const unsigned nfb = *t.fb_count;
+    const unsigned size = (unsigned)t.size;
+    // one warp per 32 bodies of a queued group
+    for (unsigned w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nfb * BPL;
+         w += warps) {
+        const int gw = t.fb_list[w / BPL];
+        {
+            const int leaf = n + gw * 32 * BPL + (int)(w % BPL) * 32 + lane;
+            const float4 me = __ldg(&t.node4[leaf]);
+            float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+            unsigned curr = 1, visits = 0;
+            unsigned long long inter = 0;
+            do {
+                const float4 nd = __ldg(&t.node4[curr]);
+                const float dx = nd.x - me.x, dy = nd.y - me.y, dz = nd.z - me.z;
+                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                if (d2 > nd.w) {
+                    float r2 = d2 + eps2;
+                    if (CLAMP) r2 = fmaxf(r2, 1e-8f);
+                    const float inv = rsqrt_mufu(r2);
+                    const float inv2 = inv * inv, inv3 = inv2 * inv;
+                    const float s3 = __ldg(&t.nodem[curr]) * inv3;
+                    float ax = dx * s3, ay = dy * s3, az = dz * s3;
+                    if (ORDER == 2 && curr < (unsigned)n) {
+                        // a += d (-3 k / r^5) - (3 / r^5) M d, k = tr M / 2 - 2.5 dMd / r^2
+                        const float4 q0 = __ldg(&t.quad[2 * curr]), q1 = __ldg(&t.quad[2 * curr + 1]);
+                        const float c3 = -3.f * inv3 * inv2;
+                        const float mx = fmaf(q1.y, dz, fmaf(q1.x, dy, q0.x * dx));
+                        const float my = fmaf(q1.z, dz, fmaf(q0.y, dy, q1.x * dx));
+                        const float mz = fmaf(q0.z, dz, fmaf(q1.z, dy, q1.y * dx));
+                        const float dmd = fmaf(dz, mz, fmaf(dy, my, dx * mx));
+                        const float ck = c3 * fmaf(-2.5f * dmd, inv2, q0.w);
+                        ax += fmaf(ck, dx, c3 * mx);
+                        ay += fmaf(ck, dy, c3 * my);
+                        az += fmaf(ck, dz, c3 * mz);
+                    }
+                    // (h, l) += p with the rounding error of h + p kept in l
+                    auto add = [](float& h, float& l, float p) {
+                        const float s = h + p, bp = s - h;
+                        l += (h - (s - bp)) + (p - bp);
+                        h = s;
+                    };
+                    add(hx, lx, ax);
+                    add(hy, ly, ay);
+                    add(hz, lz, az);
+                    ++inter;
+                    curr = (curr >> (__ffs(~curr) - 1)) + 1;  // next_down: skip the subtree
+                } else {
+                    curr = 2 * curr < size ? 2 * curr : (curr >> (__ffs(~curr) - 1)) + 1;
+                }
+                if (++visits > 2 * size) {  // cannot happen on a heap; never loop forever
+                    atomicOr(err, kDevErrWalkOverflow);
+                    break;
+                }
+            } while (curr != 1);
+            const int b = t.body_n[leaf];
+            f[b] = y[3 * n + b];
+            f[n + b] = y[4 * n + b];
+            f[2 * n + b] = y[5 * n + b];
+            f[3 * n + b] = (double)hx + (double)lx;
+            f[4 * n + b] = (double)hy + (double)ly;
+            f[5 * n + b] = (double)hz + (double)lz;
+            atomicAdd(&t.counters[1], inter);
+        }
     }
 }
 
@@ -630,9 +802,39 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
         NBG_CUDA(e, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem));
         const int warps = n / (32 * bpl);
+        // "bh.test_cap": node tests after which a group walk gives up and
+        // its bodies are walked one by one; 0 (the default) sets it to
+        // "bh.test_cap_ratio" (default 3) times the median tests of up to
+        // kCapSamples groups spread over the leaves.  Groups of one part of
+        // the system have tests within a few tens of percent of each other;
+        // only groups that mix a dense region with a sparse one (bodies far
+        // apart in the group) reach the cap.
+        t->test_cap = (unsigned long long)std::max<int64_t>(e->tune_get("bh.test_cap", 0), 0);
+        if (t->test_cap == 0) {
+            const unsigned ratio = (unsigned)std::max<int64_t>(e->tune_get("bh.test_cap_ratio", 3), 1);
+            const int samples = std::min(warps, kCapSamples);  // both powers of two
+            const size_t csmem = (size_t)kGWWarps * stack_cap * sizeof(int);
+            auto count = bpl == 2 ? bh_group_count_kernel<2> : bh_group_count_kernel<1>;
+            NBG_CUDA(e, cudaFuncSetAttribute(count, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)csmem));
+            count<<<(samples + kGWWarps - 1) / kGWWarps, kGWThreads, csmem, e->stream>>>(
+                n, warps / samples, samples, *t, stack_cap,
+                (unsigned long long)std::max(n / 4, 1 << 16));
+            NBG_LAUNCHED(e, "bh_group_count_kernel");
+            bh_test_cap_kernel<<<1, kCapSamples, 0, e->stream>>>(*t, samples, ratio);
+            NBG_LAUNCHED(e, "bh_test_cap_kernel");
+        }
+        NBG_CUDA(e, cudaMemsetAsync(t->fb_count, 0, sizeof(unsigned), e->stream));
         kern<<<(warps + kGWWarps - 1) / kGWWarps, kGWThreads, smem, e->stream>>>(
             y, f, n, eps2, *t, stack_cap, e->d_err);
         NBG_LAUNCHED(e, "bh_group_walk_kernel");
+        auto fb = order == 2
+            ? (clamp ? (bpl == 2 ? bh_body_walk_kernel<true, 2, 2> : bh_body_walk_kernel<true, 1, 2>)
+                     : (bpl == 2 ? bh_body_walk_kernel<false, 2, 2> : bh_body_walk_kernel<false, 1, 2>))
+            : (clamp ? (bpl == 2 ? bh_body_walk_kernel<true, 2, 1> : bh_body_walk_kernel<true, 1, 1>)
+                     : (bpl == 2 ? bh_body_walk_kernel<false, 2, 1> : bh_body_walk_kernel<false, 1, 1>));
+        fb<<<(unsigned)e->sm_count * 2u, 128, 0, e->stream>>>(y, f, n, eps2, *t, e->d_err);
+        NBG_LAUNCHED(e, "bh_body_walk_kernel");
         return NBG_OK;
     }
     // warps past n still walk (their lanes mirror the last body) so that
@@ -660,6 +862,18 @@ extern "C" nbg_status nbg_bh_counters(nbg_engine* e, uint64_t* visits, uint64_t*
     NBG_CUDA(e, cudaMemsetAsync(e->tree->counters, 0, 4 * sizeof(unsigned long long), e->stream));
     if (visits) *visits = h[0];
     if (interactions) *interactions = h[1];
+    return NBG_OK;
+}
+
+extern "C" nbg_status nbg_bh_fallback_groups(nbg_engine* e, uint64_t* groups) {
+    using namespace nbg;
+    if (e == nullptr || groups == nullptr) return NBG_ERR_INVALID_ARG;
+    if (e->tree == nullptr) return set_error(e, NBG_ERR_NOT_INITIALIZED, "no tree built yet");
+    unsigned long long h = 0;
+    NBG_CUDA(e, cudaMemcpyAsync(&h, e->tree->counters + 3, sizeof(h), cudaMemcpyDeviceToHost,
+                                e->stream));
+    NBG_CUDA(e, cudaStreamSynchronize(e->stream));
+    *groups = h;
     return NBG_OK;
 }
 

@@ -45,6 +45,97 @@ __global__ void init_keys_kernel(const double* __restrict__ coord, int n,
     }
 }
 
+// ---- Morton-order build (mixed precision option) ----
+__device__ __forceinline__ double order_key_inverse(uint64_t k) {
+    const uint64_t b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+    return __longlong_as_double((long long)b);
+}
+
+// box[0..2] = min order keys, box[3..5] = max order keys of x, y, z.
+__global__ void bbox_kernel(const double* __restrict__ y, int n, unsigned long long* box) {
+    unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        for (int d = 0; d < 3; ++d) {
+            const unsigned long long k = order_key(y[(size_t)d * n + i]);
+            lo[d] = min(lo[d], k);
+            hi[d] = max(hi[d], k);
+        }
+    for (int d = 0; d < 3; ++d)
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[d] = min(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+            hi[d] = max(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int d = 0; d < 3; ++d) {
+            atomicMin(&box[d], lo[d]);
+            atomicMax(&box[3 + d], hi[d]);
+        }
+}
+
+// 21 bits per axis, x in the lowest bit of every triple
+__device__ __forceinline__ uint64_t spread3(uint32_t v) {
+    uint64_t x = v & 0x1FFFFFu;
+    x = (x | (x << 32)) & 0x1F00000000FFFFull;
+    x = (x | (x << 16)) & 0x1F0000FF0000FFull;
+    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
+    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+// Hilbert index of a cell of the 2^21-per-axis grid: Skilling's transform of
+// the axes to the "transposed" index (J. Skilling, "Programming the Hilbert
+// curve", AIP Conf. Proc. 707, 2004), then the bits interleaved from the most
+// significant, axis 0 first.  Consecutive indices are adjacent cells.
+__device__ __forceinline__ uint64_t hilbert_key(uint32_t x0, uint32_t x1, uint32_t x2) {
+    uint32_t X[3] = {x0, x1, x2};
+    const uint32_t M = 1u << 20;
+    for (uint32_t Q = M; Q > 1; Q >>= 1) {  // undo excess work
+        const uint32_t P = Q - 1;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (X[i] & Q) {
+                X[0] ^= P;  // invert
+            } else {        // exchange
+                const uint32_t t = (X[0] ^ X[i]) & P;
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    X[1] ^= X[0];  // Gray encode
+    X[2] ^= X[1];
+    uint32_t t = 0;
+    for (uint32_t Q = M; Q > 1; Q >>= 1)
+        if (X[2] & Q) t ^= Q - 1;
+    X[0] ^= t;
+    X[1] ^= t;
+    X[2] ^= t;
+    return (spread3(X[0]) << 2) | (spread3(X[1]) << 1) | spread3(X[2]);
+}
+
+__global__ void morton_keys_kernel(const double* __restrict__ y, int n,
+                                   const unsigned long long* __restrict__ box,
+                                   uint64_t* __restrict__ keys, int* __restrict__ vals,
+                                   int hilbert) {
+    double lo[3], scale[3];
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = order_key_inverse(box[d]);
+        const double ext = order_key_inverse(box[3 + d]) - lo[d];
+        scale[d] = ext > 0.0 ? 2097151.0 / ext : 0.0;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t q[3];
+        for (int d = 0; d < 3; ++d) {
+            const double v = (y[(size_t)d * n + i] - lo[d]) * scale[d];
+            q[d] = (uint32_t)fmin(fmax(v, 0.0), 2097151.0);
+        }
+        keys[i] = hilbert ? hilbert_key(q[0], q[1], q[2])
+                          : spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+        vals[i] = i;
+    }
+}
+
 // Per-block digit histogram: hist[digit * nblocks + block].
 __global__ void __launch_bounds__(kSortThreads)
 radix_hist_kernel(const uint64_t* __restrict__ keys, int n, int shift, unsigned* __restrict__ hist) {
@@ -374,6 +465,10 @@ nbg_status tree_alloc(nbg_engine* e) {
     NBG_TRY(alloc(e, &t->tile_count, 2 * ntiles));
     NBG_TRY(alloc(e, &t->hist, kDigits * nblocks));
     NBG_TRY(alloc(e, &t->totals, kDigits));
+    NBG_TRY(alloc(e, &t->box, 6));
+    NBG_TRY(alloc(e, &t->fb_list, n / 32 + 1));
+    NBG_TRY(alloc(e, &t->fb_count, 1));
+    NBG_TRY(alloc(e, &t->cap_state, 1 + 256));
     NBG_TRY(alloc(e, &t->com, 3 * sz));
     NBG_TRY(alloc(e, &t->mass, sz));
     NBG_TRY(alloc(e, &t->bmin, 3 * sz));
@@ -426,7 +521,8 @@ void tree_destroy(nbg_engine* e) {
     TreeState* t = e->tree;
     if (t == nullptr) return;
     void* ptrs[] = {t->keys[0], t->keys[1], t->vals[0], t->vals[1], t->lists[0], t->lists[1],
-                    t->lists[2], t->spare[0], t->spare[1], t->flag, t->tile_count, t->hist, t->totals,
+                    t->lists[2], t->spare[0], t->spare[1], t->flag, t->tile_count, t->hist, t->totals, t->box,
+                    t->fb_list, t->fb_count, t->cap_state,
                     t->com, t->mass, t->bmin, t->bmax, t->crit2, t->body_n, t->node4,
                     t->nodem, t->feat, t->quad, t->counters};
     for (void* p : ptrs) cudaFree(p);
@@ -453,6 +549,33 @@ nbg_status tree_build(nbg_engine* e, const double* y) {
     t->lambda = e->params.distance_to_node_radius_ratio;
     ProfScope ps(e, NBG_K_TREE_BUILD);
     const unsigned g = grid_for(n, 256, (unsigned)e->sm_count * 8u);
+    // mixed precision defaults to the Hilbert tree: at equal force error
+    // its group walk does several times fewer node tests than on the kd
+    // tree, whose median cuts leave long thin cells with large radii (the
+    // learned correction keeps the kd tree it was trained and measured on)
+    const bool hilbert_default = e->params.precision != NBG_PREC_FP64 && !e->params.learned;
+    const int64_t curve = e->tune_get("bh.build", hilbert_default ? 2 : 0);
+    if (e->params.precision != NBG_PREC_FP64 && (curve == 1 || curve == 2)) {
+        // space-filling-curve order (1: Morton, 2: Hilbert): one sort; leaf p
+        // = p-th body along the curve, every node the union of its two halves
+        // (a different tree from the reference's; the FP64 path always
+        // builds the reference's)
+        const unsigned long long init[6] = {~0ull, ~0ull, ~0ull, 0ull, 0ull, 0ull};
+        NBG_CUDA(e, cudaMemcpyAsync(t->box, init, sizeof(init), cudaMemcpyHostToDevice, e->stream));
+        bbox_kernel<<<g, 256, 0, e->stream>>>(y, n, t->box);
+        NBG_LAUNCHED(e, "bbox_kernel");
+        morton_keys_kernel<<<g, 256, 0, e->stream>>>(y, n, t->box, t->keys[0], t->vals[0],
+                                                     curve == 2 ? 1 : 0);
+        NBG_LAUNCHED(e, "morton_keys_kernel");
+        nbg_status s = radix_sort(e, t, n);
+        if (s != NBG_OK) return s;
+        leaf_init_kernel<<<g, 256, 0, e->stream>>>(t->vals[0], y, e->d_mass, n, *t);
+        NBG_LAUNCHED(e, "leaf_init_kernel");
+        s = update_levels(e, t);
+        if (s != NBG_OK) return s;
+        t->built = true;
+        return NBG_OK;
+    }
     // 1. three sorted lists
     for (int d = 0; d < 3; ++d) {
         init_keys_kernel<<<g, 256, 0, e->stream>>>(y + (size_t)d * n, n, t->keys[0], t->vals[0]);

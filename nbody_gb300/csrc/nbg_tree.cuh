@@ -26,6 +26,7 @@ struct TreeState {
     int* tile_count = nullptr;               // [2][n / kPartTile + 1]
     unsigned* hist = nullptr;                // radix per-block digit counts
     unsigned* totals = nullptr;              // radix per-digit totals
+    unsigned long long* box = nullptr;       // [6] order keys of the bounding box (Morton build)
 
     // heap arrays, FP64 SoA (the reference's node fields)
     double* com = nullptr;    // [3][size] mass centre
@@ -46,13 +47,26 @@ struct TreeState {
     // quad[2 idx] = (Mxx, Myy, Mzz, tr M / 2), quad[2 idx + 1] = (Mxy, Mxz, Myz, 0)
     float4* quad = nullptr;   // [2][size] or null
 
-    // walk counters: node visits and accepted interactions (mixed walk)
+    // walk counters: node tests, interactions, deepest group-walk stack,
+    // groups handed to the per-body fallback walk
     unsigned long long* counters = nullptr;  // [4]
+
+    // group walks that exceed a node-test cap give up; their group ids go
+    // to fb_list and a per-body walk computes those bodies (nbg_bh.cu).
+    // The cap is test_cap when that is set, else cap_state[0], set from the
+    // sampled groups' test counts in cap_state[1..256].
+    int* fb_list = nullptr;                  // [n / 32]
+    unsigned* fb_count = nullptr;            // [1]
+    unsigned long long* cap_state = nullptr; // [1 + 256]
+    unsigned long long test_cap = 0;
 };
 
 constexpr int kPartTile = 2048;  // elements per partition tile (256 threads x 8)
 
-nbg_status tree_build(nbg_engine* e, const double* y);  // full kd-median build
+// Full build.  Default: the reference's kd-median tree.  With the tuning key
+// "bh.build" = 1 and mixed precision: leaves in Morton order, the list
+// halved at every level (one sort, no partitions; a different tree).
+nbg_status tree_build(nbg_engine* e, const double* y);
 nbg_status tree_refit(nbg_engine* e, const double* y);  // fixed topology, new positions
 
 }  // namespace nbg

@@ -432,6 +432,12 @@ class NbodyEngineGB300:
                         "statistics")
         return out
 
+    def bh_fallback_groups(self) -> int:
+        """Groups handed to the per-body fallback walk since the last bh_counters."""
+        g = C.c_uint64(0)
+        self._check(self._lib.nbg_bh_fallback_groups(self._h, C.byref(g)), "bh_fallback_groups")
+        return g.value
+
     def bh_stack_peak(self):
         """(deepest group-walk stack since the last bh_counters, capacity)."""
         p, c = C.c_uint64(0), C.c_uint64(0)

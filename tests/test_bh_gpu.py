@@ -187,6 +187,93 @@ def test_bh_group_walk_deep_trees(make_engine, oracle, n, kind):
     assert np.all(np.isfinite(f)) and np.median(rel) < 1e-2
 
 
+@pytest.mark.parametrize("lam", [2.0, 1.0 / 0.9])
+def test_bh_curve_builds(make_engine, oracle, lam):
+    """bh.build = 1 (Morton) and 2 (Hilbert): the leaves are the bodies in
+    curve order (a permutation) and the walk over that tree keeps the
+    accuracy of the reference's per-body walk on the kd tree at the same
+    ratio (within 1.5x at p99)."""
+    n = 16384
+    d = NBodyData.plummer(n, seed=4)
+    y = d.to_state()
+    rows = np.random.default_rng(9).choice(n, size=512, replace=False)
+    a_ref = oracle.accel_rows(y, d.mass, 0.0, rows=rows)
+    f_bh = oracle.fcompute_bh(y, d.mass, lam, layout=2, traverse=0, nthreads=8)[0]
+    rel_ref = _rel(f_bh[3 * n:].reshape(3, n).T[rows], a_ref)
+    res = {}
+    for build in (0, 1, 2):
+        e = make_engine(algo="bh", precision="mixed", softening=0.0,
+                        distance_to_node_radius_ratio=lam)
+        e.tune_set("bh.build", build)
+        assert e.init(d)
+        f = _f(e, y)
+        assert np.array_equal(f[:3 * n], y[3 * n:])
+        leaves = e.tree_leaves()
+        assert sorted(leaves.tolist()) == list(range(n))
+        res[build] = _rel(f[3 * n:].reshape(3, n).T[rows], a_ref)
+        fb_first = e.bh_fallback_groups()
+        e.bh_counters()
+        # the test cap (3x the median of sampled groups' tests) depends on
+        # the tree alone: a second call on the same state gives the same forces
+        f2 = _f(e, y)
+        fb_next = e.bh_fallback_groups()
+        print(f"\nlambda {lam:.3f} build {build}: p50 {np.median(res[build]):.2e} "
+              f"p99 {np.quantile(res[build], 0.99):.2e}; fallback groups {fb_first}, then {fb_next}")
+        assert fb_next == fb_first <= n // 64 // 10
+        assert np.array_equal(f, f2)
+    print(f"reference walk p99 {np.quantile(rel_ref, 0.99):.2e}")
+    for build in (1, 2):
+        assert np.quantile(res[build], 0.99) <= 1.5 * np.quantile(rel_ref, 0.99)
+        assert np.median(res[build]) <= 1.5 * np.median(res[0])
+
+
+@pytest.mark.parametrize("group", [64, 32])
+@pytest.mark.parametrize("order", [1, 2])
+def test_bh_body_walk_fallback(make_engine, oracle, group, order):
+    """A group walk that exceeds bh.test_cap node tests hands its bodies to
+    the per-body walk.  With a cap of one test every group does: the forces
+    are then the reference's per-body walk on the same kd tree in FP32
+    records (against the oracle's FP64 walk: equal but for the few bodies
+    where an acceptance test falls the other way in FP32), and with the
+    quadrupole term they are well below that walk's error."""
+    n = 16384
+    lam = 2.0
+    d = NBodyData.plummer(n, seed=6)
+    y = d.to_state()
+    rows = np.random.default_rng(3).choice(n, size=512, replace=False)
+    a_ref = oracle.accel_rows(y, d.mass, 0.0, rows=rows)
+    res = {}
+    for cap in (0, 1):
+        e = make_engine(algo="bh", precision="mixed", softening=0.0,
+                        distance_to_node_radius_ratio=lam)
+        e.tune_set("bh.group", group)
+        e.tune_set("bh.order", order)
+        e.tune_set("bh.build", 0)  # the reference's tree, as the oracle builds it
+        if cap:
+            e.tune_set("bh.test_cap", cap)
+        assert e.init(d)
+        f = _f(e, y)
+        assert np.array_equal(f[:3 * n], y[3 * n:])
+        assert e.bh_fallback_groups() == (n // group if cap else 0)
+        res[cap] = f
+    a_fb = res[1][3 * n:].reshape(3, n).T
+    rel = _rel(a_fb[rows], a_ref)
+    rel_gw = _rel(res[0][3 * n:].reshape(3, n).T[rows], a_ref)
+    print(f"\ngroup {group} order {order}: fallback p50 {np.median(rel):.2e} p99 "
+          f"{np.quantile(rel, 0.99):.2e}; group walk p50 {np.median(rel_gw):.2e} "
+          f"p99 {np.quantile(rel_gw, 0.99):.2e}")
+    f_bh = oracle.fcompute_bh(y, d.mass, lam, layout=2, traverse=0, nthreads=8)[0]
+    a_bh = f_bh[3 * n:].reshape(3, n).T
+    if order == 1:
+        diff = _rel(a_fb, a_bh)
+        assert np.median(diff) < 1e-5
+        assert np.mean(diff > 1e-4) < 0.02
+    else:
+        rel_bh = _rel(a_bh[rows], a_ref)
+        assert np.median(rel) < 0.5 * np.median(rel_bh)
+        assert np.quantile(rel, 0.99) < 0.7 * np.quantile(rel_bh, 0.99)
+
+
 def test_bh_mixed_refit_path(make_engine):
     n = 4096
     d = NBodyData.plummer(n, seed=5)
