@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--bh-only", action="store_true",
                     help="run only the Barnes-Hut suite (with --bh-n bodies); prints its JSON")
     ap.add_argument("--bh-n", type=int, default=1 << 20, help="bodies of the Barnes-Hut suite")
+    ap.add_argument("--bh-cases", default="",
+                    help="with --bh-only: comma-separated names of the suite's cases to run "
+                         "(e.g. hilbert_theta_0.5); default all")
     return ap.parse_args()
 
 
@@ -391,8 +394,9 @@ def train_correction(epochs: int = 8):
                "generate_s": gen_s, "train_s": train_s}
 
 
-def run_bh_suite(rank: int, n_bh: int = 1 << 20):
-    """Plummer N = 2^20, softening 1e-3, heap_stackless, rebuilt every fcompute."""
+def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
+    """Plummer N = 2^20, softening 1e-3, heap_stackless, rebuilt every fcompute.
+    `cases`: names of the cases to run (all when None)."""
     from nbody_gb300.data import NBodyData
     from oracle.oracle import load_oracle
     d = NBodyData.plummer(n_bh, seed=3)
@@ -402,34 +406,47 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20):
     res = {"workload": f"Barnes-Hut fcompute, N={n_bh} Plummer, softening 1e-3, heap_stackless, "
                        "tree rebuilt every call, FP32 walk / FP64 state",
            "error_judge": "FP64 direct sum (oracle) on 4096 sampled bodies"}
-    # the reference's kd-median tree at the reference's opening ratios, then
-    # the default Hilbert tree at the same ratios and at lambda 2.5, where
-    # both its p50 and p99 are below the kd tree's at theta 0.5
-    res["plain_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, build=0)
-    res["plain_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d, build=0)
-    res["hilbert_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d)
-    res["hilbert_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d)
-    res["hilbert_lambda_2.5"] = bench_bh(n_bh, 2.5, False, rows, a_ref, d)
-    res["morton_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, build=1)
-    res["quadrupole_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, order=2, build=0)
-    res["quadrupole_hilbert_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, order=2)
-    res["coherent_walk_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, walk=0, build=0)
-    # tree_build_rate 4 (the reference's refit option): one build and three
-    # refits per four fcomputes; same positions, so the same forces
-    res["refit_rate4_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, calls=8,
-                                            build_rate=4, build=0)
-    res["refit_rate4_hilbert_theta_0.5"] = bench_bh(n_bh, 2.0, False, rows, a_ref, d, calls=8,
-                                                    build_rate=4)
-    w, fit = train_correction()
-    res["learned_theta_0.9"] = bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=w,
-                                        build=0)
-    res["learned_theta_0.9"]["training"] = fit
-    res["accuracy_target_1e-4"] = accuracy_target(n_bh, rows, a_ref, d)
-    res["rkdp_theta_0.5"] = bh_rkdp_run(n_bh, d)
-    p05, l09 = res["plain_theta_0.5"], res["learned_theta_0.9"]
-    res["learned_0.9_vs_plain_0.5"] = {
-        "bodies_per_s_ratio": l09["bodies_per_s"] / p05["bodies_per_s"],
-        "p99_ratio": l09["p99"] / p05["p99"]}
+
+    def learned_case():
+        w, fit = train_correction()
+        r = bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=w, build=0)
+        r["training"] = fit
+        return r
+
+    suite = {
+        # the reference's kd-median tree at the reference's opening ratios,
+        # then the default Hilbert tree at the same ratios and at lambda 2.5,
+        # where both its p50 and p99 are below the kd tree's at theta 0.5
+        "plain_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, build=0),
+        "plain_theta_0.9": lambda: bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d, build=0),
+        "hilbert_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d),
+        "hilbert_theta_0.9": lambda: bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d),
+        "hilbert_lambda_2.5": lambda: bench_bh(n_bh, 2.5, False, rows, a_ref, d),
+        "morton_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, build=1),
+        "quadrupole_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, order=2,
+                                                 build=0),
+        "quadrupole_hilbert_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d,
+                                                         order=2),
+        "coherent_walk_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, walk=0,
+                                                    build=0),
+        # tree_build_rate 4 (the reference's refit option): one build and
+        # three refits per four fcomputes; same positions, so the same forces
+        "refit_rate4_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, calls=8,
+                                                  build_rate=4, build=0),
+        "refit_rate4_hilbert_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d,
+                                                          calls=8, build_rate=4),
+        "learned_theta_0.9": learned_case,
+        "accuracy_target_1e-4": lambda: accuracy_target(n_bh, rows, a_ref, d),
+        "rkdp_theta_0.5": lambda: bh_rkdp_run(n_bh, d),
+    }
+    for name, run in suite.items():
+        if cases is None or name in cases:
+            res[name] = run()
+    if "plain_theta_0.5" in res and "learned_theta_0.9" in res:
+        p05, l09 = res["plain_theta_0.5"], res["learned_theta_0.9"]
+        res["learned_0.9_vs_plain_0.5"] = {
+            "bodies_per_s_ratio": l09["bodies_per_s"] / p05["bodies_per_s"],
+            "p99_ratio": l09["p99"] / p05["p99"]}
     return res
 
 
@@ -671,7 +688,8 @@ def run_gb300(args):
 def main():
     args = parse()
     if args.bh_only:
-        print(json.dumps(run_bh_suite(0, args.bh_n)), flush=True)
+        cases = [c for c in args.bh_cases.split(",") if c] or None
+        print(json.dumps(run_bh_suite(0, args.bh_n, cases)), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -194,8 +194,8 @@ struct GroupSmem {  // followed by the stacks, kGWWarps x stack_cap ints
 
 inline int group_stack_cap(int levels) { return kGWStackPerLevel * (levels + 1) + 32; }
 
-// groups whose node tests set the group walk's test cap
-constexpr int kCapSamples = 256;
+// groups whose node tests set the group walk's test cap (one warp each, one block)
+constexpr int kCapSamples = 32;
 
 // Second list of the quadrupole walk (bh.order = 2): accepted cells with their
 // second moments; leaves stay in the monopole list.  Arrays in the order
@@ -534,29 +534,34 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
     if (lane == 0) atomicAdd(&t.counters[1], inter * 32ull * BPL);
 }
 
-// Node tests of a sample of groups (every stride-th), counted by the group
-// walk's own traversal without its force evaluation; a sample stops
-// counting past `limit`.  Their median times a ratio is the walk's test
-// cap, a function of this tree alone, so that equal trees give equal forces.
+// The group walk's test cap: ratio x the median node tests of kCapSamples
+// groups spread over the leaves (every stride-th), a function of the tree
+// alone, so that equal trees give equal forces.  One block, one warp per
+// sample, each running the group walk's traversal without its force
+// evaluation.  The samples walk in rounds of doubling test limits (4096,
+// 8192, ...) and stop once more than half have finished: the median is then
+// known without walking the samples above it, which are the slow ones.
 template <int BPL>
-__global__ void __launch_bounds__(kGWThreads)
-bh_group_count_kernel(int n, int stride, int samples, TreeState t, int stack_cap,
-                      unsigned long long limit) {
-    extern __shared__ int count_stacks[];
+__global__ void __launch_bounds__(kCapSamples * 32, 1)
+bh_test_cap_kernel(int n, int stride, int samples, TreeState t, int stack_cap, unsigned ratio) {
+    extern __shared__ int cap_stacks[];
+    __shared__ unsigned long long counts[kCapSamples];
+    __shared__ int finished[kCapSamples];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int smp = blockIdx.x * kGWWarps + warp;
-    if (smp >= samples) return;
-    const int gw = smp * stride;
+    const bool active = warp < samples;
+    const int gw = warp * stride;
     float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    if (active) {
 #pragma unroll
-    for (int b = 0; b < BPL; ++b) {
-        const float4 me = __ldg(&t.node4[n + gw * 32 * BPL + b * 32 + lane]);
-        lo[0] = fminf(lo[0], me.x);
-        lo[1] = fminf(lo[1], me.y);
-        lo[2] = fminf(lo[2], me.z);
-        hi[0] = fmaxf(hi[0], me.x);
-        hi[1] = fmaxf(hi[1], me.y);
-        hi[2] = fmaxf(hi[2], me.z);
+        for (int b = 0; b < BPL; ++b) {
+            const float4 me = __ldg(&t.node4[n + gw * 32 * BPL + b * 32 + lane]);
+            lo[0] = fminf(lo[0], me.x);
+            lo[1] = fminf(lo[1], me.y);
+            lo[2] = fminf(lo[2], me.z);
+            hi[0] = fmaxf(hi[0], me.x);
+            hi[1] = fmaxf(hi[1], me.y);
+            hi[2] = fmaxf(hi[2], me.z);
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
@@ -565,125 +570,161 @@ bh_group_count_kernel(int n, int stride, int samples, TreeState t, int stack_cap
             lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
             hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
         }
-    int* stack = count_stacks + warp * stack_cap;
+    int* stack = cap_stacks + warp * stack_cap;
     const unsigned lt = (1u << lane) - 1u;
     if (lane == 0) stack[0] = 0;
     __syncwarp();
-    int sp = 1;
-    unsigned long long tests = 0;
-    while (sp > 0 && tests <= limit) {
-        const int k = min(sp, 16);
-        int c = 0;
-        if (lane < 2 * k) c = 2 * stack[sp - 1 - (lane >> 1)] + (lane & 1);
-        __syncwarp();
-        sp -= k;
-        const bool valid = lane < 2 * k && c != 0;
-        bool open = false;
-        if (valid && c < n) {
-            const float4 nd = __ldg(&t.node4[c]);
-            const float ex = fmaxf(fmaxf(lo[0] - nd.x, nd.x - hi[0]), 0.f);
-            const float ey = fmaxf(fmaxf(lo[1] - nd.y, nd.y - hi[1]), 0.f);
-            const float ez = fmaxf(fmaxf(lo[2] - nd.z, nd.z - hi[2]), 0.f);
-            open = !(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > nd.w);
+    int sp = active ? 1 : 0;
+    unsigned long long tests = 0, limit = 4096;
+    for (int round = 0; round < 40; ++round, limit *= 2) {
+        while (sp > 0 && tests <= limit) {
+            const int k = min(sp, 16);
+            int c = 0;
+            if (lane < 2 * k) c = 2 * stack[sp - 1 - (lane >> 1)] + (lane & 1);
+            __syncwarp();
+            sp -= k;
+            const bool valid = lane < 2 * k && c != 0;
+            bool open = false;
+            if (valid && c < n) {
+                const float4 nd = __ldg(&t.node4[c]);
+                const float ex = fmaxf(fmaxf(lo[0] - nd.x, nd.x - hi[0]), 0.f);
+                const float ey = fmaxf(fmaxf(lo[1] - nd.y, nd.y - hi[1]), 0.f);
+                const float ez = fmaxf(fmaxf(lo[2] - nd.z, nd.z - hi[2]), 0.f);
+                open = !(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > nd.w);
+            }
+            tests += (unsigned long long)__popc(__ballot_sync(0xffffffffu, valid));
+            const unsigned om = __ballot_sync(0xffffffffu, open);
+            const int npush = __popc(om);
+            if (sp + npush > stack_cap) {  // the walk itself reports the overflow
+                sp = 0;
+                break;
+            }
+            if (open) stack[sp + __popc(om & lt)] = c;
+            sp += npush;
+            __syncwarp();
         }
-        tests += (unsigned long long)__popc(__ballot_sync(0xffffffffu, valid));
-        const unsigned om = __ballot_sync(0xffffffffu, open);
-        const int npush = __popc(om);
-        if (sp + npush > stack_cap) break;  // the walk itself reports an overflow
-        if (open) stack[sp + __popc(om & lt)] = c;
-        sp += npush;
-        __syncwarp();
+        if (lane == 0 && active) {
+            counts[warp] = tests;
+            finished[warp] = sp == 0;
+        }
+        __syncthreads();
+        int fin = 0;
+        for (int j = 0; j < samples; ++j) fin += finished[j];
+        if (2 * fin > samples) break;  // the same decision in every thread
+        __syncthreads();
     }
-    if (lane == 0) t.cap_state[1 + smp] = tests;
+    // finished samples hold their counts, the others a count above the last
+    // limit: the value of rank samples / 2 is the median
+    if (threadIdx.x < samples) {
+        const unsigned long long v = counts[threadIdx.x];
+        int rank = 0;
+        for (int j = 0; j < samples; ++j)
+            rank += (counts[j] < v || (counts[j] == v && j < (int)threadIdx.x)) ? 1 : 0;
+        if (rank == samples / 2) t.cap_state[0] = max((unsigned long long)ratio * v, 4096ull);
+    }
 }
 
-// The test cap: ratio x the median of the sampled counts (at least 4096).
-// One block of `samples` threads; each finds its value's rank.
-__global__ void bh_test_cap_kernel(TreeState t, int samples, unsigned ratio) {
-    const int i = threadIdx.x;
-    if (i >= samples) return;
-    const unsigned long long v = t.cap_state[1 + i];
-    int rank = 0;
-    for (int j = 0; j < samples; ++j) {
-        const unsigned long long u = t.cap_state[1 + j];
-        rank += (u < v || (u == v && j < i)) ? 1 : 0;
-    }
-    if (rank == samples / 2) t.cap_state[0] = max((unsigned long long)ratio * v, 4096ull);
-}
-
-// The bodies of the groups the group walk gave up on: one lane per body,
-// the reference's per-body stackless walk (accept when d^2 > crit^2, then
-// skip the subtree; leaves have crit^2 = 0, so a body skips itself), FP32
-// records, two-sum accumulation, the quadrupole term with ORDER 2 as in the
-// group walk.
+// The bodies of the groups the group walk gave up on, one warp per body: the
+// group walk's traversal with the body's own point as the group's box, so
+// a node is accepted when d^2 > crit^2 from the body (the reference's
+// per-body rule; leaves always, the body's own leaf adding zero), 32 node
+// tests per step.  Each lane evaluates the nodes it accepted (with the
+// quadrupole term for cells with ORDER 2) into two-sum accumulators; the
+// warp's sum is formed in FP64.
 template <bool CLAMP, int BPL, int ORDER>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kGWThreads)
 bh_body_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n, float eps2,
-                    TreeState t, unsigned* err) {
-    const int lane = threadIdx.x & 31;
-    const int warps = gridDim.x * (blockDim.x >> 5);
-    const unsigned nfb = *t.fb_count;
-    const unsigned size = (unsigned)t.size;
-    // one warp per 32 bodies of a queued group
-    for (unsigned w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nfb * BPL;
-         w += warps) {
-        const int gw = t.fb_list[w / BPL];
-        {
-            const int leaf = n + gw * 32 * BPL + (int)(w % BPL) * 32 + lane;
-            const float4 me = __ldg(&t.node4[leaf]);
-            float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
-            unsigned curr = 1, visits = 0;
-            unsigned long long inter = 0;
-            do {
-                const float4 nd = __ldg(&t.node4[curr]);
-                const float dx = nd.x - me.x, dy = nd.y - me.y, dz = nd.z - me.z;
-                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                if (d2 > nd.w) {
-                    float r2 = d2 + eps2;
-                    if (CLAMP) r2 = fmaxf(r2, 1e-8f);
-                    const float inv = rsqrt_mufu(r2);
-                    const float inv2 = inv * inv, inv3 = inv2 * inv;
-                    const float s3 = __ldg(&t.nodem[curr]) * inv3;
-                    float ax = dx * s3, ay = dy * s3, az = dz * s3;
-                    if (ORDER == 2 && curr < (unsigned)n) {
-                        // a += d (-3 k / r^5) - (3 / r^5) M d, k = tr M / 2 - 2.5 dMd / r^2
-                        const float4 q0 = __ldg(&t.quad[2 * curr]), q1 = __ldg(&t.quad[2 * curr + 1]);
-                        const float c3 = -3.f * inv3 * inv2;
-                        const float mx = fmaf(q1.y, dz, fmaf(q1.x, dy, q0.x * dx));
-                        const float my = fmaf(q1.z, dz, fmaf(q0.y, dy, q1.x * dx));
-                        const float mz = fmaf(q0.z, dz, fmaf(q1.z, dy, q1.y * dx));
-                        const float dmd = fmaf(dz, mz, fmaf(dy, my, dx * mx));
-                        const float ck = c3 * fmaf(-2.5f * dmd, inv2, q0.w);
-                        ax += fmaf(ck, dx, c3 * mx);
-                        ay += fmaf(ck, dy, c3 * my);
-                        az += fmaf(ck, dz, c3 * mz);
-                    }
-                    // (h, l) += p with the rounding error of h + p kept in l
-                    auto add = [](float& h, float& l, float p) {
-                        const float s = h + p, bp = s - h;
-                        l += (h - (s - bp)) + (p - bp);
-                        h = s;
-                    };
-                    add(hx, lx, ax);
-                    add(hy, ly, ay);
-                    add(hz, lz, az);
-                    ++inter;
-                    curr = (curr >> (__ffs(~curr) - 1)) + 1;  // next_down: skip the subtree
-                } else {
-                    curr = 2 * curr < size ? 2 * curr : (curr >> (__ffs(~curr) - 1)) + 1;
+                    TreeState t, int stack_cap, unsigned* err) {
+    extern __shared__ int body_stacks[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    int* stack = body_stacks + warp * stack_cap;
+    const unsigned bodies = *t.fb_count * 32u * BPL;
+    const unsigned warps = gridDim.x * kGWWarps;
+    for (unsigned w = blockIdx.x * kGWWarps + warp; w < bodies; w += warps) {
+        const int gw = t.fb_list[w / (32 * BPL)];
+        const int leaf = n + gw * 32 * BPL + (int)(w % (32 * BPL));
+        const float4 me = __ldg(&t.node4[leaf]);
+        float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+        // (h, l) += p with the rounding error of h + p kept in l
+        auto add = [](float& h, float& l, float p) {
+            const float s = h + p, bp = s - h;
+            l += (h - (s - bp)) + (p - bp);
+            h = s;
+        };
+        unsigned long long inter = 0;
+        __syncwarp();
+        if (lane == 0) stack[0] = 0;
+        __syncwarp();
+        int sp = 1;
+        while (sp > 0) {
+            const int k = min(sp, 16);
+            int c = 0;
+            if (lane < 2 * k) c = 2 * stack[sp - 1 - (lane >> 1)] + (lane & 1);
+            __syncwarp();
+            sp -= k;
+            const bool valid = lane < 2 * k && c != 0;
+            bool accept = false, open = false;
+            float dx = 0.f, dy = 0.f, dz = 0.f;
+            if (valid) {
+                const float4 nd = __ldg(&t.node4[c]);
+                dx = nd.x - me.x;
+                dy = nd.y - me.y;
+                dz = nd.z - me.z;
+                accept = c >= n || fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > nd.w;
+                open = !accept;
+            }
+            if (accept) {
+                float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+                if (CLAMP) r2 = fmaxf(r2, 1e-8f);
+                const float inv = rsqrt_mufu(r2);
+                const float inv2 = inv * inv, inv3 = inv2 * inv;
+                const float s3 = __ldg(&t.nodem[c]) * inv3;
+                float ax = dx * s3, ay = dy * s3, az = dz * s3;
+                if (ORDER == 2 && c < n) {
+                    // a += d (-3 k / r^5) - (3 / r^5) M d, k = tr M / 2 - 2.5 dMd / r^2
+                    const float4 q0 = __ldg(&t.quad[2 * c]), q1 = __ldg(&t.quad[2 * c + 1]);
+                    const float c3 = -3.f * inv3 * inv2;
+                    const float mx = fmaf(q1.y, dz, fmaf(q1.x, dy, q0.x * dx));
+                    const float my = fmaf(q1.z, dz, fmaf(q0.y, dy, q1.x * dx));
+                    const float mz = fmaf(q0.z, dz, fmaf(q1.z, dy, q1.y * dx));
+                    const float dmd = fmaf(dz, mz, fmaf(dy, my, dx * mx));
+                    const float ck = c3 * fmaf(-2.5f * dmd, inv2, q0.w);
+                    ax += fmaf(ck, dx, c3 * mx);
+                    ay += fmaf(ck, dy, c3 * my);
+                    az += fmaf(ck, dz, c3 * mz);
                 }
-                if (++visits > 2 * size) {  // cannot happen on a heap; never loop forever
-                    atomicOr(err, kDevErrWalkOverflow);
-                    break;
-                }
-            } while (curr != 1);
+                add(hx, lx, ax);
+                add(hy, ly, ay);
+                add(hz, lz, az);
+            }
+            inter += (unsigned long long)__popc(__ballot_sync(0xffffffffu, accept));
+            const unsigned om = __ballot_sync(0xffffffffu, open);
+            const int npush = __popc(om);
+            if (sp + npush > stack_cap) {  // beyond 48 entries per level: reported, never written
+                if (lane == 0) atomicOr(err, kDevErrWalkOverflow);
+                break;
+            }
+            if (open) stack[sp + __popc(om & lt)] = c;
+            sp += npush;
+            __syncwarp();
+        }
+        double ax = (double)hx + (double)lx, ay = (double)hy + (double)ly;
+        double az = (double)hz + (double)lz;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            ax += __shfl_xor_sync(0xffffffffu, ax, o);
+            ay += __shfl_xor_sync(0xffffffffu, ay, o);
+            az += __shfl_xor_sync(0xffffffffu, az, o);
+        }
+        if (lane == 0) {
             const int b = t.body_n[leaf];
             f[b] = y[3 * n + b];
             f[n + b] = y[4 * n + b];
             f[2 * n + b] = y[5 * n + b];
-            f[3 * n + b] = (double)hx + (double)lx;
-            f[4 * n + b] = (double)hy + (double)ly;
-            f[5 * n + b] = (double)hz + (double)lz;
+            f[3 * n + b] = ax;
+            f[4 * n + b] = ay;
+            f[5 * n + b] = az;
             atomicAdd(&t.counters[1], inter);
         }
     }
@@ -804,7 +845,7 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
         const int warps = n / (32 * bpl);
         // "bh.test_cap": node tests after which a group walk gives up and
         // its bodies are walked one by one; 0 (the default) sets it to
-        // "bh.test_cap_ratio" (default 3) times the median tests of up to
+        // "bh.test_cap_ratio" (default 3) times the median tests of
         // kCapSamples groups spread over the leaves.  Groups of one part of
         // the system have tests within a few tens of percent of each other;
         // only groups that mix a dense region with a sparse one (bodies far
@@ -813,15 +854,12 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
         if (t->test_cap == 0) {
             const unsigned ratio = (unsigned)std::max<int64_t>(e->tune_get("bh.test_cap_ratio", 3), 1);
             const int samples = std::min(warps, kCapSamples);  // both powers of two
-            const size_t csmem = (size_t)kGWWarps * stack_cap * sizeof(int);
-            auto count = bpl == 2 ? bh_group_count_kernel<2> : bh_group_count_kernel<1>;
-            NBG_CUDA(e, cudaFuncSetAttribute(count, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            const size_t csmem = (size_t)kCapSamples * stack_cap * sizeof(int);
+            auto capk = bpl == 2 ? bh_test_cap_kernel<2> : bh_test_cap_kernel<1>;
+            NBG_CUDA(e, cudaFuncSetAttribute(capk, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)csmem));
-            count<<<(samples + kGWWarps - 1) / kGWWarps, kGWThreads, csmem, e->stream>>>(
-                n, warps / samples, samples, *t, stack_cap,
-                (unsigned long long)std::max(n / 4, 1 << 16));
-            NBG_LAUNCHED(e, "bh_group_count_kernel");
-            bh_test_cap_kernel<<<1, kCapSamples, 0, e->stream>>>(*t, samples, ratio);
+            capk<<<1, kCapSamples * 32, csmem, e->stream>>>(n, warps / samples, samples, *t,
+                                                            stack_cap, ratio);
             NBG_LAUNCHED(e, "bh_test_cap_kernel");
         }
         NBG_CUDA(e, cudaMemsetAsync(t->fb_count, 0, sizeof(unsigned), e->stream));
@@ -833,7 +871,10 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
                      : (bpl == 2 ? bh_body_walk_kernel<false, 2, 2> : bh_body_walk_kernel<false, 1, 2>))
             : (clamp ? (bpl == 2 ? bh_body_walk_kernel<true, 2, 1> : bh_body_walk_kernel<true, 1, 1>)
                      : (bpl == 2 ? bh_body_walk_kernel<false, 2, 1> : bh_body_walk_kernel<false, 1, 1>));
-        fb<<<(unsigned)e->sm_count * 2u, 128, 0, e->stream>>>(y, f, n, eps2, *t, e->d_err);
+        const size_t fsmem = (size_t)kGWWarps * stack_cap * sizeof(int);
+        NBG_CUDA(e, cudaFuncSetAttribute(fb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+        fb<<<(unsigned)e->sm_count * 8u, kGWThreads, fsmem, e->stream>>>(y, f, n, eps2, *t, stack_cap,
+                                                                     e->d_err);
         NBG_LAUNCHED(e, "bh_body_walk_kernel");
         return NBG_OK;
     }

@@ -468,7 +468,7 @@ nbg_status tree_alloc(nbg_engine* e) {
     NBG_TRY(alloc(e, &t->box, 6));
     NBG_TRY(alloc(e, &t->fb_list, n / 32 + 1));
     NBG_TRY(alloc(e, &t->fb_count, 1));
-    NBG_TRY(alloc(e, &t->cap_state, 1 + 256));
+    NBG_TRY(alloc(e, &t->cap_state, 1));
     NBG_TRY(alloc(e, &t->com, 3 * sz));
     NBG_TRY(alloc(e, &t->mass, sz));
     NBG_TRY(alloc(e, &t->bmin, 3 * sz));

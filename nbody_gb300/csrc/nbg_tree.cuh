@@ -54,10 +54,10 @@ struct TreeState {
     // group walks that exceed a node-test cap give up; their group ids go
     // to fb_list and a per-body walk computes those bodies (nbg_bh.cu).
     // The cap is test_cap when that is set, else cap_state[0], set from the
-    // sampled groups' test counts in cap_state[1..256].
+    // test counts of sampled groups by bh_test_cap_kernel.
     int* fb_list = nullptr;                  // [n / 32]
     unsigned* fb_count = nullptr;            // [1]
-    unsigned long long* cap_state = nullptr; // [1 + 256]
+    unsigned long long* cap_state = nullptr; // [1]
     unsigned long long test_cap = 0;
 };
 
