@@ -845,14 +845,14 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
         const int warps = n / (32 * bpl);
         // "bh.test_cap": node tests after which a group walk gives up and
         // its bodies are walked one by one; 0 (the default) sets it to
-        // "bh.test_cap_ratio" (default 3) times the median tests of
+        // "bh.test_cap_ratio" (default 2) times the median tests of
         // kCapSamples groups spread over the leaves.  Groups of one part of
         // the system have tests within a few tens of percent of each other;
         // only groups that mix a dense region with a sparse one (bodies far
         // apart in the group) reach the cap.
         t->test_cap = (unsigned long long)std::max<int64_t>(e->tune_get("bh.test_cap", 0), 0);
         if (t->test_cap == 0) {
-            const unsigned ratio = (unsigned)std::max<int64_t>(e->tune_get("bh.test_cap_ratio", 3), 1);
+            const unsigned ratio = (unsigned)std::max<int64_t>(e->tune_get("bh.test_cap_ratio", 2), 1);
             const int samples = std::min(warps, kCapSamples);  // both powers of two
             const size_t csmem = (size_t)kCapSamples * stack_cap * sizeof(int);
             auto capk = bpl == 2 ? bh_test_cap_kernel<2> : bh_test_cap_kernel<1>;

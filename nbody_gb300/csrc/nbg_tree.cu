@@ -20,6 +20,7 @@
 //     non-contracting build of the reference bit for bit.
 // With distinct coordinates the subsets equal nth_element's; the whole tree,
 // and therefore every acceptance decision of the walk, matches the reference.
+#include <algorithm>
 #include <cstring>
 
 #include "nbg_tree.cuh"
@@ -408,10 +409,11 @@ __device__ __forceinline__ double len3(double x, double y, double z) {
 }
 
 // One level of the bottom-up update (nbody/nbody_space_heap.cpp:119-134).
-__global__ void update_level_kernel(int first, int count, double lambda2, TreeState t) {
+// One inner node from its two children (nbody/nbody_space_heap.cpp:119-134),
+// FP64 with the reference's roundings.
+__device__ __forceinline__ void update_node(size_t idx, double lambda2, TreeState& t) {
     const size_t sz = t.size;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
-        const size_t idx = (size_t)first + k;
+    {
         const size_t l = 2 * idx, r = 2 * idx + 1;
         const double ml = t.mass[l], mr = t.mass[r];
         const double m = __dadd_rn(ml, mr);
@@ -488,9 +490,11 @@ nbg_status tree_alloc(nbg_engine* e) {
     return NBG_OK;
 }
 
-nbg_status radix_sort(nbg_engine* e, TreeState* t, int n) {
+// Stable LSD sort of keys[0] / vals[0] by the key bits from 8 * first_pass
+// up (an even number of passes, so the result is back in keys[0] / vals[0]).
+nbg_status radix_sort(nbg_engine* e, TreeState* t, int n, int first_pass = 0) {
     const int nblocks = (n + kSortTile - 1) / kSortTile;
-    for (int pass = 0; pass < 8; ++pass) {
+    for (int pass = first_pass; pass < 8; ++pass) {
         const int shift = 8 * pass;
         const int src = pass & 1, dst = src ^ 1;
         radix_hist_kernel<<<nblocks, kSortThreads, 0, e->stream>>>(t->keys[src], n, shift, t->hist);
@@ -501,16 +505,34 @@ nbg_status radix_sort(nbg_engine* e, TreeState* t, int n) {
             t->keys[src], t->vals[src], t->keys[dst], t->vals[dst], n, shift, t->hist, t->totals);
         NBG_LAUNCHED(e, "radix_scatter_kernel");
     }
-    return NBG_OK;  // 8 passes: the result is back in keys[0] / vals[0]
+    return NBG_OK;
+}
+
+// Levels [lv_lo, lv_hi) of the heap, bottom-up, in one launch: block b owns
+// the subtree under node 2^lv_lo + b down to level lv_hi - 1 (at most
+// kFusedLevels levels, 256 nodes at its bottom), with a block barrier
+// between levels; global writes of one level are visible to the block's
+// reads of the next.  The per-node arithmetic is update_node's.
+constexpr int kFusedLevels = 9;
+
+__global__ void __launch_bounds__(256)
+update_levels_fused_kernel(int lv_lo, int lv_hi, double lambda2, TreeState t) {
+    const size_t root = ((size_t)1 << lv_lo) + blockIdx.x;
+    for (int lv = lv_hi - 1; lv >= lv_lo; --lv) {
+        const int span = 1 << (lv - lv_lo);
+        const size_t first = root << (lv - lv_lo);
+        for (int k = threadIdx.x; k < span; k += blockDim.x) update_node(first + k, lambda2, t);
+        __syncthreads();
+    }
 }
 
 nbg_status update_levels(nbg_engine* e, TreeState* t) {
     const double lambda2 = t->lambda * t->lambda;
-    for (int lv = t->levels - 1; lv >= 0; --lv) {
-        const int first = 1 << lv;
-        update_level_kernel<<<grid_for(first, 256, (unsigned)e->sm_count * 8u), 256, 0,
-                              e->stream>>>(first, first, lambda2, *t);
-        NBG_LAUNCHED(e, "update_level_kernel");
+    for (int hi = t->levels; hi > 0;) {
+        const int lo = std::max(0, hi - kFusedLevels);
+        update_levels_fused_kernel<<<1u << lo, 256, 0, e->stream>>>(lo, hi, lambda2, *t);
+        NBG_LAUNCHED(e, "update_levels_fused_kernel");
+        hi = lo;
     }
     return NBG_OK;
 }
@@ -560,14 +582,17 @@ nbg_status tree_build(nbg_engine* e, const double* y) {
         // = p-th body along the curve, every node the union of its two halves
         // (a different tree from the reference's; the FP64 path always
         // builds the reference's)
-        const unsigned long long init[6] = {~0ull, ~0ull, ~0ull, 0ull, 0ull, 0ull};
-        NBG_CUDA(e, cudaMemcpyAsync(t->box, init, sizeof(init), cudaMemcpyHostToDevice, e->stream));
+        // box = {min keys: all ones, max keys: zero}
+        NBG_CUDA(e, cudaMemsetAsync(t->box, 0xFF, 3 * sizeof(unsigned long long), e->stream));
+        NBG_CUDA(e, cudaMemsetAsync(t->box + 3, 0, 3 * sizeof(unsigned long long), e->stream));
         bbox_kernel<<<g, 256, 0, e->stream>>>(y, n, t->box);
         NBG_LAUNCHED(e, "bbox_kernel");
         morton_keys_kernel<<<g, 256, 0, e->stream>>>(y, n, t->box, t->keys[0], t->vals[0],
                                                      curve == 2 ? 1 : 0);
         NBG_LAUNCHED(e, "morton_keys_kernel");
-        nbg_status s = radix_sort(e, t, n);
+        // the top 48 key bits (16 per axis): cells of 2^-16 of the box,
+        // bodies sharing one in index order
+        nbg_status s = radix_sort(e, t, n, 2);
         if (s != NBG_OK) return s;
         leaf_init_kernel<<<g, 256, 0, e->stream>>>(t->vals[0], y, e->d_mass, n, *t);
         NBG_LAUNCHED(e, "leaf_init_kernel");
