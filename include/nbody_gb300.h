@@ -251,6 +251,9 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       mixed precision: 1 leaves in Morton order, 2 in Hilbert order (the
  *       default without the learned correction), every node the two halves of its range -- one sort
  *       instead of three, a different tree with compact cells),
+ *       "bh.fp64_nodes" (mixed precision: 1 forms the FP64 node arrays as
+ *       the FP64 path does; default 0, only the FP32 records the mixed walks
+ *       read, from FP32 bounding boxes),
  *       "bh.test_cap" (node tests after which a group walk hands its bodies
  *       to the per-body walk; 0, the default, is "bh.test_cap_ratio"
  *       (default 3) times the previous walk's mean per group),

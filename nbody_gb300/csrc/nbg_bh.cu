@@ -784,7 +784,8 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
     const int n = (int)e->count;
     const uint64_t rate = e->params.tree_build_rate;
     const bool build = e->tree == nullptr || !e->tree->built || rate == 0 || step % rate == 0;
-    nbg_status s = build ? tree_build(e, y) : tree_refit(e, y);
+    nbg_status s = build ? tree_build(e, y, e->params.precision == NBG_PREC_FP64 || e->params.learned)
+                         : tree_refit(e, y);
     if (s != NBG_OK) return s;
     TreeState* t = e->tree;
     ProfScope ps(e, NBG_K_BH_WALK);

@@ -932,7 +932,7 @@ nbg_status nbg_learn_generate(nbg_engine* e, size_t max_samples, uint64_t seed,
     if (s != NBG_OK) return s;
     LearnState* L = e->learn;
     const double* y = static_cast<const double*>(e->y->dptr);
-    s = tree_build(e, y);
+    s = tree_build(e, y, true);
     if (s != NBG_OK) return s;
     s = tree_features(e);
     if (s != NBG_OK) return s;

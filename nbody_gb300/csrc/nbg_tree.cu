@@ -360,6 +360,7 @@ __global__ void __launch_bounds__(256) part_scatter_kernel(PartArgs a) {
 }
 
 // Leaves: leaf n + p holds body list[p] (nbody/nbody_space_heap.cpp:141-148).
+template <bool F32>
 __global__ void leaf_init_kernel(const int* __restrict__ order, const double* __restrict__ y,
                                  const double* __restrict__ mass, int n, TreeState t) {
     const size_t sz = t.size;
@@ -368,6 +369,14 @@ __global__ void leaf_init_kernel(const int* __restrict__ order, const double* __
         const size_t idx = (size_t)n + p;
         t.body_n[idx] = b;
         const double x = y[b], yy = y[n + b], z = y[2 * n + b];
+        if (F32) {
+            const float4 v = make_float4((float)x, (float)yy, (float)z, 0.f);
+            t.node4[idx] = v;
+            t.nodem[idx] = (float)mass[b];
+            t.box4[idx] = v;
+            t.box4[sz + idx] = v;
+            continue;
+        }
         t.com[idx] = x;
         t.com[sz + idx] = yy;
         t.com[2 * sz + idx] = z;
@@ -385,12 +394,20 @@ __global__ void leaf_init_kernel(const int* __restrict__ order, const double* __
 }
 
 // Refit leaves: new positions, same bodies (nbody/nbody_space_heap.cpp:45-53).
+template <bool F32>
 __global__ void leaf_refit_kernel(const double* __restrict__ y, int n, TreeState t) {
     const size_t sz = t.size;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const size_t idx = (size_t)n + p;
         const int b = t.body_n[idx];
         const double x = y[b], yy = y[n + b], z = y[2 * n + b];
+        if (F32) {
+            const float4 v = make_float4((float)x, (float)yy, (float)z, 0.f);
+            t.node4[idx] = v;
+            t.box4[idx] = v;
+            t.box4[sz + idx] = v;
+            continue;
+        }
         t.com[idx] = x;
         t.com[sz + idx] = yy;
         t.com[2 * sz + idx] = z;
@@ -442,6 +459,28 @@ __device__ __forceinline__ void update_node(size_t idx, double lambda2, TreeStat
     }
 }
 
+// The same node update in FP32 from the FP32 records and boxes (mixed
+// precision, whose walks read only the FP32 records).
+__device__ __forceinline__ void update_node_f32(size_t idx, float lambda2, TreeState& t) {
+    const size_t sz = t.size;
+    const size_t l = 2 * idx, r = 2 * idx + 1;
+    const float4 cl = t.node4[l], cr = t.node4[r];
+    const float ml = t.nodem[l], mr = t.nodem[r];
+    const float m = ml + mr;
+    const float4 ll = t.box4[l], lr = t.box4[r], hl = t.box4[sz + l], hr = t.box4[sz + r];
+    const float cx = (cl.x * ml + cr.x * mr) / m, cy = (cl.y * ml + cr.y * mr) / m;
+    const float cz = (cl.z * ml + cr.z * mr) / m;
+    const float lx = fminf(ll.x, lr.x), ly = fminf(ll.y, lr.y), lz = fminf(ll.z, lr.z);
+    const float hx = fmaxf(hl.x, hr.x), hy = fmaxf(hl.y, hr.y), hz = fmaxf(hl.z, hr.z);
+    const float ex = hx - lx, ey = hy - ly, ez = hz - lz;
+    const float ox = 0.5f * (hx + lx) - cx, oy = 0.5f * (hy + ly) - cy, oz = 0.5f * (hz + lz) - cz;
+    const float rr = 0.5f * sqrtf(ex * ex + ey * ey + ez * ez) + sqrtf(ox * ox + oy * oy + oz * oz);
+    t.node4[idx] = make_float4(cx, cy, cz, rr * rr * lambda2);
+    t.nodem[idx] = m;
+    t.box4[idx] = make_float4(lx, ly, lz, 0.f);
+    t.box4[sz + idx] = make_float4(hx, hy, hz, 0.f);
+}
+
 template <typename T>
 nbg_status alloc(nbg_engine* e, T** p, size_t count) {
     NBG_CUDA(e, cudaMalloc(p, count * sizeof(T) + 256));
@@ -479,6 +518,7 @@ nbg_status tree_alloc(nbg_engine* e) {
     NBG_TRY(alloc(e, &t->body_n, sz));
     NBG_TRY(alloc(e, &t->node4, sz));
     NBG_TRY(alloc(e, &t->nodem, sz));
+    NBG_TRY(alloc(e, &t->box4, 2 * sz));
     NBG_TRY(alloc(e, &t->counters, 4));
 #undef NBG_TRY
     // index 0 is unused; zero everything once so stray reads are defined
@@ -515,13 +555,17 @@ nbg_status radix_sort(nbg_engine* e, TreeState* t, int n, int first_pass = 0) {
 // reads of the next.  The per-node arithmetic is update_node's.
 constexpr int kFusedLevels = 9;
 
+template <bool F32>
 __global__ void __launch_bounds__(256)
 update_levels_fused_kernel(int lv_lo, int lv_hi, double lambda2, TreeState t) {
     const size_t root = ((size_t)1 << lv_lo) + blockIdx.x;
     for (int lv = lv_hi - 1; lv >= lv_lo; --lv) {
         const int span = 1 << (lv - lv_lo);
         const size_t first = root << (lv - lv_lo);
-        for (int k = threadIdx.x; k < span; k += blockDim.x) update_node(first + k, lambda2, t);
+        for (int k = threadIdx.x; k < span; k += blockDim.x) {
+            if (F32) update_node_f32(first + k, (float)lambda2, t);
+            else update_node(first + k, lambda2, t);
+        }
         __syncthreads();
     }
 }
@@ -530,7 +574,10 @@ nbg_status update_levels(nbg_engine* e, TreeState* t) {
     const double lambda2 = t->lambda * t->lambda;
     for (int hi = t->levels; hi > 0;) {
         const int lo = std::max(0, hi - kFusedLevels);
-        update_levels_fused_kernel<<<1u << lo, 256, 0, e->stream>>>(lo, hi, lambda2, *t);
+        if (t->f32)
+            update_levels_fused_kernel<true><<<1u << lo, 256, 0, e->stream>>>(lo, hi, lambda2, *t);
+        else
+            update_levels_fused_kernel<false><<<1u << lo, 256, 0, e->stream>>>(lo, hi, lambda2, *t);
         NBG_LAUNCHED(e, "update_levels_fused_kernel");
         hi = lo;
     }
@@ -546,13 +593,13 @@ void tree_destroy(nbg_engine* e) {
                     t->lists[2], t->spare[0], t->spare[1], t->flag, t->tile_count, t->hist, t->totals, t->box,
                     t->fb_list, t->fb_count, t->cap_state,
                     t->com, t->mass, t->bmin, t->bmax, t->crit2, t->body_n, t->node4,
-                    t->nodem, t->feat, t->quad, t->counters};
+                    t->nodem, t->box4, t->feat, t->quad, t->counters};
     for (void* p : ptrs) cudaFree(p);
     delete t;
     e->tree = nullptr;
 }
 
-nbg_status tree_build(nbg_engine* e, const double* y) {
+nbg_status tree_build(nbg_engine* e, const double* y, bool fp64_nodes) {
     const int n = (int)e->count;
     if (e->tree == nullptr) {
         e->tree = new TreeState();
@@ -569,6 +616,8 @@ nbg_status tree_build(nbg_engine* e, const double* y) {
     }
     TreeState* t = e->tree;
     t->lambda = e->params.distance_to_node_radius_ratio;
+    // "bh.fp64_nodes" = 1 keeps the FP64 node update in mixed precision
+    t->f32 = !fp64_nodes && e->tune_get("bh.fp64_nodes", 0) == 0;
     ProfScope ps(e, NBG_K_TREE_BUILD);
     const unsigned g = grid_for(n, 256, (unsigned)e->sm_count * 8u);
     // mixed precision defaults to the Hilbert tree: at equal force error
@@ -594,7 +643,10 @@ nbg_status tree_build(nbg_engine* e, const double* y) {
         // bodies sharing one in index order
         nbg_status s = radix_sort(e, t, n, 2);
         if (s != NBG_OK) return s;
-        leaf_init_kernel<<<g, 256, 0, e->stream>>>(t->vals[0], y, e->d_mass, n, *t);
+        if (t->f32)
+            leaf_init_kernel<true><<<g, 256, 0, e->stream>>>(t->vals[0], y, e->d_mass, n, *t);
+        else
+            leaf_init_kernel<false><<<g, 256, 0, e->stream>>>(t->vals[0], y, e->d_mass, n, *t);
         NBG_LAUNCHED(e, "leaf_init_kernel");
         s = update_levels(e, t);
         if (s != NBG_OK) return s;
@@ -642,7 +694,10 @@ nbg_status tree_build(nbg_engine* e, const double* y) {
         t->spare[1] = tmp1;
     }
     // 3. leaves, then the bottom-up update
-    leaf_init_kernel<<<g, 256, 0, e->stream>>>(t->lists[0], y, e->d_mass, n, *t);
+    if (t->f32)
+        leaf_init_kernel<true><<<g, 256, 0, e->stream>>>(t->lists[0], y, e->d_mass, n, *t);
+    else
+        leaf_init_kernel<false><<<g, 256, 0, e->stream>>>(t->lists[0], y, e->d_mass, n, *t);
     NBG_LAUNCHED(e, "leaf_init_kernel");
     nbg_status s = update_levels(e, t);
     if (s != NBG_OK) return s;
@@ -655,7 +710,11 @@ nbg_status tree_refit(nbg_engine* e, const double* y) {
     const int n = (int)e->count;
     t->lambda = e->params.distance_to_node_radius_ratio;
     ProfScope ps(e, NBG_K_TREE_BUILD);
-    leaf_refit_kernel<<<grid_for(n, 256, (unsigned)e->sm_count * 8u), 256, 0, e->stream>>>(y, n, *t);
+    const unsigned g = grid_for(n, 256, (unsigned)e->sm_count * 8u);
+    if (t->f32)
+        leaf_refit_kernel<true><<<g, 256, 0, e->stream>>>(y, n, *t);
+    else
+        leaf_refit_kernel<false><<<g, 256, 0, e->stream>>>(y, n, *t);
     NBG_LAUNCHED(e, "leaf_refit_kernel");
     return update_levels(e, t);
 }

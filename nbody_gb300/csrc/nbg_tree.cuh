@@ -39,6 +39,11 @@ struct TreeState {
     // FP32 node records for the mixed-precision walk: (com.xyz, crit2), mass
     float4* node4 = nullptr;  // [size]
     float* nodem = nullptr;   // [size]
+    // f32: the last build formed only the FP32 records, from FP32 boxes
+    // (box4[node] = min corner, box4[size + node] = max corner); the FP64
+    // arrays above are then not current
+    bool f32 = false;
+    float4* box4 = nullptr;   // [2][size]
 
     // learned-correction node features (quadrupole, spread), see nbg_learned.cu
     float4* feat = nullptr;   // [3][size] or null
@@ -66,7 +71,9 @@ constexpr int kPartTile = 2048;  // elements per partition tile (256 threads x 8
 // Full build.  Default: the reference's kd-median tree.  With the tuning key
 // "bh.build" = 1 and mixed precision: leaves in Morton order, the list
 // halved at every level (one sort, no partitions; a different tree).
-nbg_status tree_build(nbg_engine* e, const double* y);
+// fp64_nodes: form the FP64 node arrays (the FP64 walk, the learned
+// correction's features); otherwise only the FP32 records
+nbg_status tree_build(nbg_engine* e, const double* y, bool fp64_nodes);
 nbg_status tree_refit(nbg_engine* e, const double* y);  // fixed topology, new positions
 
 }  // namespace nbg

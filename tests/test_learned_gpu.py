@@ -177,7 +177,8 @@ def test_learned_walk_vs_plain(make_engine, oracle, trained, group):
     def run(lam, learned):
         e = _bh_engine(make_engine, lam, learned=learned)
         e.tune_set("bh.walk", 0)  # the walk the learned path extends
-        e.tune_set("bh.build", 0)  # on the kd tree the learned path keeps
+        e.tune_set("bh.build", 0)  # on the kd tree the learned path keeps,
+        e.tune_set("bh.fp64_nodes", 1)  # with its FP64 node update
         assert e.init(d)
         if learned:
             e.learn_set_weights(w)
