@@ -269,11 +269,11 @@ __device__ __forceinline__ void group_pair(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f
 // SMACC: the per-body two-sum accumulators (6 BPL packed values per lane)
 // live in shared memory instead of registers; they are touched once per list
 // evaluation, and the registers they free allow more resident warps.
-template <bool CLAMP, int MINB, int BPL, int ORDER, int EUNR = 2, bool SMACC = false>
-__global__ void __launch_bounds__(kGWThreads, MINB)
-bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n, float eps2v,
-                     TreeState t, int stack_cap, unsigned* err) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+template <bool CLAMP, int BPL, int ORDER, int EUNR, bool SMACC>
+__device__ __forceinline__ void group_walk_one(const double* __restrict__ y, double* __restrict__ f,
+                                               int n, float eps2v, const TreeState& t,
+                                               int stack_cap, unsigned* err,
+                                               unsigned char* smem_raw, const int gw) {
     GroupSmem& S = *reinterpret_cast<GroupSmem*>(smem_raw);
     QuadLists& Q = *reinterpret_cast<QuadLists*>(smem_raw + sizeof(GroupSmem));
     int* stacks = reinterpret_cast<int*>(smem_raw + sizeof(GroupSmem) +
@@ -286,8 +286,6 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
         else return acc_reg[q];
     };
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int gw = blockIdx.x * kGWWarps + warp;
-    if (gw * 32 * BPL >= n) return;  // n is a power of two >= 32 BPL: groups are full
     float4 me[BPL];
 #pragma unroll
     for (int b = 0; b < BPL; ++b) me[b] = __ldg(&t.node4[n + gw * 32 * BPL + b * 32 + lane]);
@@ -532,6 +530,28 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
         f[5 * n + b] = ((double)h0 + (double)h1) + ((double)l0 + (double)l1);
     }
     if (lane == 0) atomicAdd(&t.counters[1], inter * 32ull * BPL);
+}
+
+// Persistent over the groups (n is a power of two >= 32 BPL, so groups are
+// full): each warp starts at its own group and then takes the next untaken
+// one from a counter, so the last groups spread over all warps instead of
+// leaving a partial wave.  A group's forces do not depend on which warp
+// computes it.
+template <bool CLAMP, int MINB, int BPL, int ORDER, int EUNR = 2, bool SMACC = false>
+__global__ void __launch_bounds__(kGWThreads, MINB)
+bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n, float eps2v,
+                     TreeState t, int stack_cap, unsigned* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31;
+    const int groups = n / (32 * BPL);
+    int gw = blockIdx.x * kGWWarps + (threadIdx.x >> 5);
+    while (gw < groups) {
+        group_walk_one<CLAMP, BPL, ORDER, EUNR, SMACC>(y, f, n, eps2v, t, stack_cap, err, smem_raw,
+                                                      gw);
+        int next = 0;
+        if (lane == 0) next = (int)atomicAdd(&t.fb_count[1], 1u);
+        gw = gridDim.x * kGWWarps + __shfl_sync(0xffffffffu, next, 0);
+    }
 }
 
 // The group walk's test cap: ratio x the median node tests of kCapSamples
@@ -863,9 +883,17 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
                                                             stack_cap, ratio);
             NBG_LAUNCHED(e, "bh_test_cap_kernel");
         }
-        NBG_CUDA(e, cudaMemsetAsync(t->fb_count, 0, sizeof(unsigned), e->stream));
-        kern<<<(warps + kGWWarps - 1) / kGWWarps, kGWThreads, smem, e->stream>>>(
-            y, f, n, eps2, *t, stack_cap, e->d_err);
+        // fb_count[0]: groups handed to the fallback, [1]: the walk's next group
+        NBG_CUDA(e, cudaMemsetAsync(t->fb_count, 0, 2 * sizeof(unsigned), e->stream));
+        // "bh.persistent" (default 1): as many CTAs as fit at once; 0: one
+        // CTA per kGWWarps groups
+        unsigned blocks = (unsigned)((warps + kGWWarps - 1) / kGWWarps);
+        if (e->tune_get("bh.persistent", 1) != 0) {
+            int per_sm = 0;
+            NBG_CUDA(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kGWThreads, smem));
+            blocks = std::min(blocks, (unsigned)std::max(per_sm, 1) * (unsigned)e->sm_count);
+        }
+        kern<<<blocks, kGWThreads, smem, e->stream>>>(y, f, n, eps2, *t, stack_cap, e->d_err);
         NBG_LAUNCHED(e, "bh_group_walk_kernel");
         auto fb = order == 2
             ? (clamp ? (bpl == 2 ? bh_body_walk_kernel<true, 2, 2> : bh_body_walk_kernel<true, 1, 2>)

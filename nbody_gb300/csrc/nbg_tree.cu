@@ -508,7 +508,7 @@ nbg_status tree_alloc(nbg_engine* e) {
     NBG_TRY(alloc(e, &t->totals, kDigits));
     NBG_TRY(alloc(e, &t->box, 6));
     NBG_TRY(alloc(e, &t->fb_list, n / 32 + 1));
-    NBG_TRY(alloc(e, &t->fb_count, 1));
+    NBG_TRY(alloc(e, &t->fb_count, 2));
     NBG_TRY(alloc(e, &t->cap_state, 1));
     NBG_TRY(alloc(e, &t->com, 3 * sz));
     NBG_TRY(alloc(e, &t->mass, sz));

@@ -61,7 +61,7 @@ struct TreeState {
     // The cap is test_cap when that is set, else cap_state[0], set from the
     // test counts of sampled groups by bh_test_cap_kernel.
     int* fb_list = nullptr;                  // [n / 32]
-    unsigned* fb_count = nullptr;            // [1]
+    unsigned* fb_count = nullptr;            // [2]: queued groups, the walk's next group
     unsigned long long* cap_state = nullptr; // [1]
     unsigned long long test_cap = 0;
 };
