@@ -639,8 +639,8 @@ nbg_status tree_build(nbg_engine* e, const double* y, bool fp64_nodes) {
         morton_keys_kernel<<<g, 256, 0, e->stream>>>(y, n, t->box, t->keys[0], t->vals[0],
                                                      curve == 2 ? 1 : 0);
         NBG_LAUNCHED(e, "morton_keys_kernel");
-        // the top 48 key bits (16 per axis): cells of 2^-16 of the box,
-        // bodies sharing one in index order
+        // the key bits from 16 up (47 of 63: the curve down to cells of
+        // about 2^-16 of the box per axis), bodies sharing one in index order
         nbg_status s = radix_sort(e, t, n, 2);
         if (s != NBG_OK) return s;
         if (t->f32)

@@ -227,6 +227,31 @@ def test_bh_curve_builds(make_engine, oracle, lam):
         assert np.median(res[build]) <= 1.5 * np.median(res[0])
 
 
+@pytest.mark.parametrize("kind", ["plummer", "cube"])
+@pytest.mark.parametrize("build", [1, 2])
+def test_bh_curve_leaf_order(make_engine, build, kind):
+    """The Morton (1) and Hilbert (2) builds put the bodies in the leaves in
+    exactly the order of the CPU restatement (tests/curve_order.py: box,
+    21-bit cells, keys, stable sort on the key bits from 16 up), and a refit
+    keeps that order."""
+    from tests import curve_order as C
+    n = 8192
+    d = NBodyData.plummer(n, seed=12) if kind == "plummer" else \
+        NBodyData.uniform_cube(n, side=3.0, seed=12)
+    e = make_engine(algo="bh", precision="mixed", softening=1e-3,
+                    distance_to_node_radius_ratio=2.0, tree_build_rate=2)
+    e.tune_set("bh.build", build)
+    assert e.init(d)
+    y = d.to_state()
+    e.set_step(0)
+    _f(e, y)
+    expect = C.leaf_order(d.vertices, hilbert=build == 2)
+    assert np.array_equal(e.tree_leaves(), expect)
+    e.set_step(1)  # refit: same leaves
+    _f(e, y * 1.01)
+    assert np.array_equal(e.tree_leaves(), expect)
+
+
 @pytest.mark.parametrize("group", [64, 32])
 @pytest.mark.parametrize("order", [1, 2])
 def test_bh_body_walk_fallback(make_engine, oracle, group, order):
