@@ -464,6 +464,26 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
     return res
 
 
+def bh_summary(bh):
+    """The Barnes-Hut figures of the headline metric, picked from the suite:
+    bodies/s at p99 <= 1e-4 (and 1e-2, 1e-3) and theta = 0.5 on both trees."""
+    if not bh:
+        return None
+    out = {}
+    fr = bh.get("accuracy_frontier")
+    if fr:
+        for tgt, b in fr["best"].items():
+            if b["best"]:
+                out[f"p99_le_{tgt}"] = {"path": b["best"]["path"], "ms": b["best"]["ms"],
+                                        "bodies_per_s": b["bodies_per_s"],
+                                        "speedup_vs_reference_method":
+                                            b["speedup_vs_reference_method"]}
+    for k in ("hilbert_theta_0.5", "plain_theta_0.5", "learned_theta_0.9"):
+        if k in bh:
+            out[k] = {x: bh[k][x] for x in ("ms_per_fcompute", "bodies_per_s", "p50", "p99")}
+    return out
+
+
 def run_stats_bench(n: int = N_BODIES):
     """P, L, E, V of one state (the run's conservation check): the GPU's FP64 reductions
     against the reference's single-threaded host sums (nbody/nbody_data.cpp:
@@ -493,7 +513,7 @@ def run_stats_bench(n: int = N_BODIES):
             "cpu_sample": f"{m} bodies, scaled by (N / {m})^2"}
 
 
-def run_ensemble_suite(steps: int = 20):
+def run_ensemble_suite(steps: int = 20, peak_flops: float = None):
     """2048 Plummer clusters, N_s ~ U{64..4096} (seeded), softening 1e-3,
     rkdp per-system control (tolerance 1e-8), one graph per step."""
     from nbody_gb300.data import NBodyData
@@ -530,6 +550,7 @@ def run_ensemble_suite(steps: int = 20):
             "accepted_fraction": accepted / (2048 * steps),
             "ms_per_step": wall / steps * 1e3,
             "pairs_per_s": pairs / wall,
+            "fp32_fraction": (pairs / wall * FLOP_PER_PAIR / peak_flops) if peak_flops else None,
             "energy_drift_median": float(np.median(drift)),
             "energy_drift_max": float(drift.max()),
             "autotuner": {"best": tuning["best"],
@@ -652,7 +673,8 @@ def run_gb300(args):
                "sample": f"block engine (FP64) on {rows} of {n} rows x {n} bodies, {dt:.1f} s"}
 
     bh = run_bh_suite(rank, args.bh_n) if (rank == 0 and not args.no_bh) else None
-    ensemble = run_ensemble_suite() if (rank == 0 and not args.no_ensemble) else None
+    ensemble = run_ensemble_suite(peak_flops=peak_flops) \
+        if (rank == 0 and not args.no_ensemble) else None
     stats = run_stats_bench(n) if (rank == 0 and not args.no_ensemble) else None
 
     if rank == 0:
@@ -686,6 +708,7 @@ def run_gb300(args):
             "gpu_launches": int(launches),
             "clocks": clk,
             "force_error": err,
+            "bh_summary": bh_summary(bh),
             "bh": bh,
             "statistics": stats,
             "ensemble": ensemble,
