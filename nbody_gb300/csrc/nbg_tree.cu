@@ -66,11 +66,22 @@ __global__ void bbox_kernel(const double* __restrict__ y, int n, unsigned long l
             lo[d] = min(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
             hi[d] = max(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
         }
+    // one atomic per CTA and bound: the six addresses are shared by all CTAs
+    __shared__ unsigned long long part[6][32];
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if ((threadIdx.x & 31) == 0)
         for (int d = 0; d < 3; ++d) {
-            atomicMin(&box[d], lo[d]);
-            atomicMax(&box[3 + d], hi[d]);
+            part[d][w] = lo[d];
+            part[3 + d][w] = hi[d];
         }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int d = threadIdx.x;
+        unsigned long long v = part[d][0];
+        for (int k = 1; k < nw; ++k) v = d < 3 ? min(v, part[d][k]) : max(v, part[d][k]);
+        if (d < 3) atomicMin(&box[d], v);
+        else atomicMax(&box[d], v);
+    }
 }
 
 // 21 bits per axis, x in the lowest bit of every triple
@@ -119,12 +130,17 @@ __global__ void morton_keys_kernel(const double* __restrict__ y, int n,
                                    const unsigned long long* __restrict__ box,
                                    uint64_t* __restrict__ keys, int* __restrict__ vals,
                                    int hilbert) {
-    double lo[3], scale[3];
-    for (int d = 0; d < 3; ++d) {
-        lo[d] = order_key_inverse(box[d]);
-        const double ext = order_key_inverse(box[3 + d]) - lo[d];
-        scale[d] = ext > 0.0 ? 2097151.0 / ext : 0.0;
+    // the box's corner and scale, once per CTA
+    __shared__ double s_lo[3], s_scale[3];
+    if (threadIdx.x < 3) {
+        const int d = threadIdx.x;
+        s_lo[d] = order_key_inverse(box[d]);
+        const double ext = order_key_inverse(box[3 + d]) - s_lo[d];
+        s_scale[d] = ext > 0.0 ? 2097151.0 / ext : 0.0;
     }
+    __syncthreads();
+    const double lo[3] = {s_lo[0], s_lo[1], s_lo[2]};
+    const double scale[3] = {s_scale[0], s_scale[1], s_scale[2]};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t q[3];
         for (int d = 0; d < 3; ++d) {
@@ -634,7 +650,7 @@ nbg_status tree_build(nbg_engine* e, const double* y, bool fp64_nodes) {
         // box = {min keys: all ones, max keys: zero}
         NBG_CUDA(e, cudaMemsetAsync(t->box, 0xFF, 3 * sizeof(unsigned long long), e->stream));
         NBG_CUDA(e, cudaMemsetAsync(t->box + 3, 0, 3 * sizeof(unsigned long long), e->stream));
-        bbox_kernel<<<g, 256, 0, e->stream>>>(y, n, t->box);
+        bbox_kernel<<<std::min(g, (unsigned)e->sm_count * 2u), 256, 0, e->stream>>>(y, n, t->box);
         NBG_LAUNCHED(e, "bbox_kernel");
         morton_keys_kernel<<<g, 256, 0, e->stream>>>(y, n, t->box, t->keys[0], t->vals[0],
                                                      curve == 2 ? 1 : 0);
