@@ -667,8 +667,10 @@ nbg_status tree_build(nbg_engine* e, const double* y, bool fp64_nodes) {
         s = update_levels(e, t);
         if (s != NBG_OK) return s;
         t->built = true;
+        t->curve = (int)curve;
         return NBG_OK;
     }
+    t->curve = 0;
     // 1. three sorted lists
     for (int d = 0; d < 3; ++d) {
         init_keys_kernel<<<g, 256, 0, e->stream>>>(y + (size_t)d * n, n, t->keys[0], t->vals[0]);

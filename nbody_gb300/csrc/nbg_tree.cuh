@@ -15,6 +15,7 @@ struct TreeState {
     size_t size = 0;  // heap size = 2n
     int levels = 0;   // K = log2(n)
     bool built = false;
+    int curve = 0;    // leaf order of the last build: 0 kd-median, 1 Morton, 2 Hilbert
     double lambda = 0.0;
 
     // build scratch
