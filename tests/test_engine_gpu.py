@@ -92,7 +92,8 @@ def test_fmadd(eng):
     assert np.all(np.abs((b + c * 5.0) - res) <= EPS)
 
 
-@pytest.mark.parametrize("csize", [1, 3, 7, 20])
+# 35 terms: the stage count of the reference's rkfeagin14 table
+@pytest.mark.parametrize("csize", [1, 3, 7, 20, 35])
 def test_fmaddn_inplace(eng, csize):
     rng = np.random.default_rng(3 + csize)
     n = eng.problem_size()
@@ -113,7 +114,7 @@ def test_fmaddn_inplace(eng, csize):
     assert np.all(np.abs((a + (b * c[:, None]).sum(axis=0)) - res) <= EPS)
 
 
-@pytest.mark.parametrize("dsize", [1, 3, 7, 20])
+@pytest.mark.parametrize("dsize", [1, 3, 7, 20, 35])
 @pytest.mark.parametrize("null_b", [False, True])
 def test_fmaddn(eng, dsize, null_b):
     rng = np.random.default_rng(11 + dsize)
