@@ -873,10 +873,9 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
         // apart in the group) reach the cap.  Such groups come from the jumps
         // of a curve order; a kd-median tree's groups are subtrees, whose
         // tests stay within a few tens of percent of each other, so there
-        // the cap is max(N / 4, 2^16) and the pre-pass is skipped.
+        // the walk is not capped and the pre-pass is skipped.
         t->test_cap = (unsigned long long)std::max<int64_t>(e->tune_get("bh.test_cap", 0), 0);
-        if (t->test_cap == 0 && t->curve == 0)
-            t->test_cap = (unsigned long long)std::max(n / 4, 1 << 16);
+        if (t->test_cap == 0 && t->curve == 0) t->test_cap = ~0ull;
         if (t->test_cap == 0) {
             const unsigned ratio = (unsigned)std::max<int64_t>(e->tune_get("bh.test_cap_ratio", 2), 1);
             const int samples = std::min(warps, kCapSamples);  // both powers of two
