@@ -443,6 +443,8 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
                                                          order=2),
         "coherent_walk_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, walk=0,
                                                     build=0),
+        "coherent_walk_hilbert_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d,
+                                                            walk=0),
         # tree_build_rate 4 (the reference's refit option): one build and
         # three refits per four fcomputes; same positions, so the same forces
         "refit_rate4_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, calls=8,
