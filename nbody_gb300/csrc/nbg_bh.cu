@@ -845,12 +845,21 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
             kern = bpl == 2 ? (clamp ? bh_group_walk_kernel<true, 4, 2, 2> : bh_group_walk_kernel<false, 4, 2, 2>)
                             : (clamp ? bh_group_walk_kernel<true, 5, 1, 2> : bh_group_walk_kernel<false, 5, 1, 2>);
         else if (acc_smem) {
-            // accumulators in shared memory (4 or 5 CTAs per SM)
+            // accumulators in shared memory (4 or 5 CTAs per SM); at 5 CTAs
+            // "bh.eval_unroll" 1, 2 (default) or 4 quads per list step
             smem += (size_t)kGWThreads * 6 * 2 * sizeof(f2_t);
-            kern = clamp ? (wb >= 5 ? bh_group_walk_kernel<true, 5, 2, 1, 2, true>
-                                    : bh_group_walk_kernel<true, 4, 2, 1, 2, true>)
-                         : (wb >= 5 ? bh_group_walk_kernel<false, 5, 2, 1, 2, true>
-                                    : bh_group_walk_kernel<false, 4, 2, 1, 2, true>);
+            const int64_t eu = e->tune_get("bh.eval_unroll", 2);
+            if (wb >= 5 && eu >= 4)
+                kern = clamp ? bh_group_walk_kernel<true, 5, 2, 1, 4, true>
+                             : bh_group_walk_kernel<false, 5, 2, 1, 4, true>;
+            else if (wb >= 5 && eu <= 1)
+                kern = clamp ? bh_group_walk_kernel<true, 5, 2, 1, 1, true>
+                             : bh_group_walk_kernel<false, 5, 2, 1, 1, true>;
+            else
+                kern = clamp ? (wb >= 5 ? bh_group_walk_kernel<true, 5, 2, 1, 2, true>
+                                        : bh_group_walk_kernel<true, 4, 2, 1, 2, true>)
+                             : (wb >= 5 ? bh_group_walk_kernel<false, 5, 2, 1, 2, true>
+                                        : bh_group_walk_kernel<false, 4, 2, 1, 2, true>);
         } else if (bpl == 2 && wb <= 4 && e->tune_get("bh.eval_unroll", 2) != 2) {
             // list-evaluation unroll of the default 64-body build
             const bool u4 = e->tune_get("bh.eval_unroll", 2) >= 4;

@@ -86,6 +86,9 @@ extern "C" nbg_status nbg_autotune(nbg_engine* e, int reps, char* report, size_t
     } else if (e->params.algo == NBG_ALGO_BH) {
         for (int b : {5, 4})
             cands.push_back({{"bh.walk", 1}, {"bh.group", 64}, {"bh.walk_blocks", b}, {"bh.acc_smem", 1}});
+        for (int u : {1, 4})
+            cands.push_back({{"bh.walk", 1}, {"bh.group", 64}, {"bh.walk_blocks", 5}, {"bh.acc_smem", 1},
+                             {"bh.eval_unroll", u}});
         for (int b : {4, 5})
             cands.push_back({{"bh.walk", 1}, {"bh.group", 64}, {"bh.walk_blocks", b}, {"bh.acc_smem", 0}});
         for (int u : {1, 4})
