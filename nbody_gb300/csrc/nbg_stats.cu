@@ -99,9 +99,14 @@ __device__ __forceinline__ double rsqrt_fp64(double x) {
 }
 
 // Potential energy: one CTA per (system, 256 i-bodies); FP64 pair sums over
-// j-tiles in shared memory, each unordered pair once (j tiles from the
-// CTA's own on; pairs in later tiles count twice, the potential being
-// symmetric); one atomicAdd per CTA into PE[s] (pre-halved).
+// j-tiles in shared memory, each unordered pair once.  With B blocks in a
+// system, block b takes the tiles b, b+1, ..., b+B/2 (mod B): its own tile
+// (both orders of each pair, weight 1), then tiles at distances 1 .. B/2
+// (one order, weight 2, the potential being symmetric); for even B the tile
+// at distance B/2 is shared by two blocks and only the lower one takes it.
+// Every CTA of a system does the same work.  One atomicAdd per CTA into
+// PE[s] (pre-halved).
+template <bool SOFT>
 __global__ void __launch_bounds__(kStatThreads)
 stats_potential_kernel(const double* __restrict__ y, const double* __restrict__ mass, size_t stride,
                        const long long* __restrict__ off, const int* __restrict__ cnt,
@@ -117,7 +122,11 @@ stats_potential_kernel(const double* __restrict__ y, const double* __restrict__ 
     const size_t i = (size_t)(o + (live ? li : 0));
     const double xi = y[i], yi = y[stride + i], zi = y[2 * stride + i], mi = live ? mass[i] : 0.0;
     double pe = 0.0;
-    for (int j0 = u.i0; j0 < n; j0 += kStatThreads) {
+    const int nb = (n + kStatThreads - 1) / kStatThreads;
+    const int bi = u.i0 / kStatThreads;
+    const int last = (nb % 2 == 0 && bi >= nb / 2) ? nb / 2 - 1 : nb / 2;
+    for (int t = 0; t <= last; ++t) {
+        const int j0 = ((bi + t) % nb) * kStatThreads;
         const int lj = j0 + threadIdx.x;
         __syncthreads();
         if (lj < n) {
@@ -129,16 +138,25 @@ stats_potential_kernel(const double* __restrict__ y, const double* __restrict__ 
         }
         __syncthreads();
         const int c = min(kStatThreads, n - j0);
-        const bool own = j0 == u.i0;
+        const bool own = t == 0;
         double tile = 0.0;
-        for (int k = 0; k < c; ++k) {
-            if (own && j0 + k == li) continue;
+        // the own tile skips the self pair; without softening, pairs closer
+        // than kMinDistance add nothing
+        auto term = [&](int k) {
             const double dx = xi - tx[k], dy = yi - ty[k], dz = zi - tz[k];
             const double r2 = dx * dx + dy * dy + dz * dz;
-            if (eps2 == 0.0 && r2 < kMinDistance) continue;
-            tile -= tm[k] * rsqrt_fp64(r2 + eps2);
+            if (!SOFT && r2 < kMinDistance) return 0.0;
+            return tm[k] * rsqrt_fp64(r2 + eps2);
+        };
+        if (own) {
+            for (int k = 0; k < c; ++k)
+                if (j0 + k != li) tile -= term(k);
+            pe += tile;
+        } else {
+#pragma unroll 4
+            for (int k = 0; k < c; ++k) tile -= term(k);
+            pe += 2.0 * tile;
         }
-        pe += own ? tile : 2.0 * tile;
     }
     const double tot = block_sum(pe * mi, sh);
     if (threadIdx.x == 0) atomicAdd(out + 12 * (size_t)u.sys + 7, tot / 2);
@@ -162,8 +180,9 @@ nbg_status stats_segments(nbg_engine* e, const double* y, const double* mass, si
     stats_linear_kernel<<<nsys, kStatThreads, 0, e->stream>>>(y, mass, stride, d_off, d_cnt, d_out);
     NBG_LAUNCHED(e, "stats_linear_kernel");
     if (!units.empty()) {
-        stats_potential_kernel<<<(unsigned)units.size(), kStatThreads, 0, e->stream>>>(
-            y, mass, stride, d_off, d_cnt, d_units, eps2, d_out);
+        auto kern = eps2 > 0.0 ? stats_potential_kernel<true> : stats_potential_kernel<false>;
+        kern<<<(unsigned)units.size(), kStatThreads, 0, e->stream>>>(y, mass, stride, d_off, d_cnt,
+                                                                     d_units, eps2, d_out);
         NBG_LAUNCHED(e, "stats_potential_kernel");
     }
     NBG_CUDA(e, cudaStreamSynchronize(e->stream));
