@@ -252,6 +252,43 @@ def test_bh_curve_leaf_order(make_engine, build, kind):
     assert np.array_equal(e.tree_leaves(), expect)
 
 
+def test_bh_hilbert_clustered_and_degenerate(make_engine, oracle):
+    """The default mixed path on inputs that stress the curve order: two dense
+    clusters far apart plus a sparse halo (groups that straddle the curve's
+    jumps between them go to the per-body walk), and a system whose bodies
+    all sit at one point.  Forces stay finite and, for the clusters, at
+    least as accurate as the reference's per-body walk at the same ratio."""
+    n = 16384
+    rng = np.random.default_rng(17)
+    a = NBodyData.plummer(7936, seed=31, scale=0.01)
+    b = NBodyData.plummer(7936, seed=32, scale=0.01)
+    halo = rng.uniform(-20.0, 20.0, size=(n - 2 * 7936, 3))
+    pos = np.concatenate([a.vertices + [5.0, 0, 0], b.vertices - [5.0, 0, 0], halo])
+    vel = np.zeros_like(pos)
+    d = NBodyData(vertices=pos, velocities=vel, mass=np.full(n, 1.0 / n))
+    y = d.to_state()
+    e = make_engine(algo="bh", precision="mixed", softening=0.0, distance_to_node_radius_ratio=2.0)
+    assert e.init(d)
+    f = _f(e, y)
+    fb = e.bh_fallback_groups()
+    assert np.all(np.isfinite(f)) and np.array_equal(f[:3 * n], y[3 * n:])
+    rows = np.random.default_rng(5).choice(n, size=512, replace=False)
+    a_ref = oracle.accel_rows(y, d.mass, 0.0, rows=rows)
+    rel = _rel(f[3 * n:].reshape(3, n).T[rows], a_ref)
+    f_bh = oracle.fcompute_bh(y, d.mass, 2.0, layout=2, traverse=0, nthreads=8)[0]
+    rel_ref = _rel(f_bh[3 * n:].reshape(3, n).T[rows], a_ref)
+    print(f"\nclusters + halo: fallback groups {fb}; p50 {np.median(rel):.2e} "
+          f"p99 {np.quantile(rel, 0.99):.2e} (reference walk p99 {np.quantile(rel_ref, 0.99):.2e})")
+    assert np.quantile(rel, 0.99) <= np.quantile(rel_ref, 0.99)
+    # every body at one point: no direction, zero force
+    n = 1024
+    d = NBodyData(vertices=np.ones((n, 3)), velocities=np.zeros((n, 3)), mass=np.full(n, 1.0 / n))
+    e = make_engine(algo="bh", precision="mixed", softening=0.0, distance_to_node_radius_ratio=2.0)
+    assert e.init(d)
+    f = _f(e, d.to_state())
+    assert np.all(f[3 * n:] == 0.0)
+
+
 @pytest.mark.parametrize("group", [64, 32])
 @pytest.mark.parametrize("order", [1, 2])
 def test_bh_body_walk_fallback(make_engine, oracle, group, order):
