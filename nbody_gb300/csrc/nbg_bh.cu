@@ -307,6 +307,14 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
             lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
             hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
         }
+    // the box as centre and half extent: the nearest point's offset on an
+    // axis is max(|x - centre| - half, 0)
+    float cb[3], hb[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        cb[a] = 0.5f * (lo[a] + hi[a]);
+        hb[a] = 0.5f * (hi[a] - lo[a]);
+    }
     int* stack = stacks + warp * stack_cap;
     float* lx = S.lx[warp];
     float* ly = S.ly[warp];
@@ -422,16 +430,15 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
         sp -= k;
         const bool valid = lane < 2 * k && c != 0;
         bool accept = false, open = false;
-        float4 nd = make_float4(0.f, 0.f, 0.f, 0.f);
-        float ndm = 0.f;
-        float4 nq0 = make_float4(0.f, 0.f, 0.f, 0.f), nq1 = nq0;
-        if (valid) {  // issued before a full list is evaluated, which covers their latency
-            nd = __ldg(&t.node4[c]);
-            ndm = __ldg(&t.nodem[c]);
-            if (ORDER == 2 && c < n) {
-                nq0 = __ldg(&t.quad[2 * c]);
-                nq1 = __ldg(&t.quad[2 * c + 1]);
-            }
+        // issued before a full list is evaluated, which covers their latency;
+        // lanes past the popped entries read record 0 (unused, zeroed), and
+        // leaves' second moments are zero
+        const float4 nd = __ldg(&t.node4[c]);
+        const float ndm = __ldg(&t.nodem[c]);
+        float4 nq0, nq1;
+        if (ORDER == 2) {
+            nq0 = __ldg(&t.quad[2 * c]);
+            nq1 = __ldg(&t.quad[2 * c + 1]);
         }
         if (lc > kGWList - 32) evaluate();  // room for this step's entries
         if (ORDER == 2 && qc > kGWQList - 32) evaluate_quad();
@@ -439,15 +446,17 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
             if (c >= n) {
                 accept = true;
             } else {
-                const float ex = fmaxf(fmaxf(lo[0] - nd.x, nd.x - hi[0]), 0.f);
-                const float ey = fmaxf(fmaxf(lo[1] - nd.y, nd.y - hi[1]), 0.f);
-                const float ez = fmaxf(fmaxf(lo[2] - nd.z, nd.z - hi[2]), 0.f);
+                const float ex = fmaxf(fabsf(nd.x - cb[0]) - hb[0], 0.f);
+                const float ey = fmaxf(fabsf(nd.y - cb[1]) - hb[1], 0.f);
+                const float ez = fmaxf(fabsf(nd.z - cb[2]) - hb[2], 0.f);
                 const float dmin2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
                 accept = dmin2 > nd.w;
                 open = !accept;
             }
         }
-        tests += (unsigned long long)__popc(__ballot_sync(0xffffffffu, valid));
+        // every popped entry stands for two tested children, except the root's
+        // stand-in entry 0 at the first step (its child 0 is not a node)
+        tests += (unsigned long long)(2 * k);
         if (tests > test_cap) {  // a group spread over much of the system:
             abandoned = true;      // its bodies are walked one by one instead
             break;
@@ -499,6 +508,7 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
     if (overflow) {
         if (lane == 0) atomicOr(err, kDevErrWalkOverflow);
     }
+    tests -= 1;  // child 0 of the first step
     if (lane == 0) {
         atomicAdd(&t.counters[0], tests);
         atomicMax(&t.counters[2], (unsigned long long)peak);
@@ -590,6 +600,12 @@ bh_test_cap_kernel(int n, int stride, int samples, TreeState t, int stack_cap, u
             lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
             hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
         }
+    float cb[3], hb[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        cb[a] = 0.5f * (lo[a] + hi[a]);
+        hb[a] = 0.5f * (hi[a] - lo[a]);
+    }
     int* stack = cap_stacks + warp * stack_cap;
     const unsigned lt = (1u << lane) - 1u;
     if (lane == 0) stack[0] = 0;
@@ -607,9 +623,9 @@ bh_test_cap_kernel(int n, int stride, int samples, TreeState t, int stack_cap, u
             bool open = false;
             if (valid && c < n) {
                 const float4 nd = __ldg(&t.node4[c]);
-                const float ex = fmaxf(fmaxf(lo[0] - nd.x, nd.x - hi[0]), 0.f);
-                const float ey = fmaxf(fmaxf(lo[1] - nd.y, nd.y - hi[1]), 0.f);
-                const float ez = fmaxf(fmaxf(lo[2] - nd.z, nd.z - hi[2]), 0.f);
+                const float ex = fmaxf(fabsf(nd.x - cb[0]) - hb[0], 0.f);
+                const float ey = fmaxf(fabsf(nd.y - cb[1]) - hb[1], 0.f);
+                const float ez = fmaxf(fabsf(nd.z - cb[2]) - hb[2], 0.f);
                 open = !(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > nd.w);
             }
             tests += (unsigned long long)__popc(__ballot_sync(0xffffffffu, valid));
