@@ -203,28 +203,35 @@ radix_digit_scan_kernel(unsigned* __restrict__ hist, int nblocks, unsigned* __re
 // Stable scatter.  Each warp owns 256 consecutive keys of the tile and walks
 // them in 8 rounds of 32; __match_any_sync ranks equal digits inside a round,
 // per-warp digit counters carry the rank across rounds, and a per-digit
-// prefix over the warps orders the warps.  Order inside the tile is kept.
+// prefix over the warps orders the warps.  The tile is first sorted by digit
+// in shared memory, then written out in that order, so that neighbouring
+// threads store to neighbouring places of a digit's run.  Order inside the
+// tile is kept.
 __global__ void __launch_bounds__(kSortThreads)
 radix_scatter_kernel(const uint64_t* __restrict__ kin, const int* __restrict__ vin,
                      uint64_t* __restrict__ kout, int* __restrict__ vout, int n, int shift,
                      const unsigned* __restrict__ offsets, const unsigned* __restrict__ totals) {
     constexpr int kWarpsS = kSortThreads / 32;
     __shared__ unsigned cnt[kWarpsS][kDigits];
-    __shared__ unsigned digit_base[kDigits];
-    // exclusive prefix of the digit totals (Hillis-Steele, one digit per thread)
+    __shared__ unsigned gbase[kDigits];  // global start of this block's run of each digit
+    __shared__ unsigned lbase[kDigits];  // start of each digit in the block's sorted tile
+    __shared__ uint64_t skey[kSortTile];
+    __shared__ int sval[kSortTile];
     static_assert(kDigits == kSortThreads, "one digit per thread");
-    {
-        const unsigned own = totals[threadIdx.x];
-        digit_base[threadIdx.x] = own;
+    // exclusive prefix of a per-digit value over the digits (Hillis-Steele)
+    auto digit_scan = [&](unsigned own, unsigned* buf) {
+        buf[threadIdx.x] = own;
         __syncthreads();
         for (int o = 1; o < kDigits; o <<= 1) {
-            const unsigned v = threadIdx.x >= (unsigned)o ? digit_base[threadIdx.x - o] : 0u;
+            const unsigned v = threadIdx.x >= (unsigned)o ? buf[threadIdx.x - o] : 0u;
             __syncthreads();
-            digit_base[threadIdx.x] += v;
+            buf[threadIdx.x] += v;
             __syncthreads();
         }
-        digit_base[threadIdx.x] -= own;  // inclusive -> exclusive
-    }
+        buf[threadIdx.x] -= own;  // inclusive -> exclusive
+        __syncthreads();
+    };
+    digit_scan(totals[threadIdx.x], gbase);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int d = lane; d < kDigits; d += 32) cnt[warp][d] = 0;
     __syncwarp();
@@ -252,23 +259,38 @@ radix_scatter_kernel(const uint64_t* __restrict__ kin, const int* __restrict__ v
         __syncwarp();
     }
     __syncthreads();
-    // per-digit prefix over warps (warp order = key order inside the tile)
-    for (int d = threadIdx.x; d < kDigits; d += kSortThreads) {
-        unsigned run = digit_base[d] + offsets[d * gridDim.x + blockIdx.x];
+    // per digit: warps' exclusive offsets inside the digit's run (warp order =
+    // key order inside the tile), the block's global start of the run
+    unsigned tot = 0;
+    {
+        const int d = threadIdx.x;
         for (int w = 0; w < kWarpsS; ++w) {
             const unsigned c = cnt[w][d];
-            cnt[w][d] = run;
-            run += c;
+            cnt[w][d] = tot;
+            tot += c;
         }
+        gbase[d] += offsets[d * gridDim.x + blockIdx.x];
     }
-    __syncthreads();
+    digit_scan(tot, lbase);
+    // the tile sorted by digit in shared memory (stable) ...
 #pragma unroll
     for (int r = 0; r < kSortItems; ++r) {
         if (dig[r] < (unsigned)kDigits) {
-            const unsigned dst = cnt[warp][dig[r]] + rank[r];
-            kout[dst] = key[r];
-            vout[dst] = val[r];
+            const unsigned li = lbase[dig[r]] + cnt[warp][dig[r]] + rank[r];
+            skey[li] = key[r];
+            sval[li] = val[r];
         }
+    }
+    __syncthreads();
+    // ... then written out in that order: consecutive threads write
+    // consecutive places of each digit's run
+    const int live = min(kSortTile, n - blockIdx.x * kSortTile);
+    for (int j = threadIdx.x; j < live; j += kSortThreads) {
+        const uint64_t k = skey[j];
+        const unsigned d = (unsigned)(k >> shift) & 0xFFu;
+        const unsigned dst = gbase[d] + (unsigned)j - lbase[d];
+        kout[dst] = k;
+        vout[dst] = sval[j];
     }
 }
 
