@@ -105,10 +105,12 @@ def test_engine_autotune_bh(make_engine):
     keys = [c["keys"] for c in rep["candidates"]]
     g64 = {"bh.walk": 1, "bh.group": 64}
     assert keys[:2] == [dict(g64, **{"bh.walk_blocks": b, "bh.acc_smem": 1}) for b in (5, 4)]
-    assert keys[2:4] == [dict(g64, **{"bh.walk_blocks": b, "bh.acc_smem": 0}) for b in (4, 5)]
-    assert keys[4:6] == [dict(g64, **{"bh.walk_blocks": 4, "bh.acc_smem": 0, "bh.eval_unroll": u})
+    assert keys[2:4] == [dict(g64, **{"bh.walk_blocks": 5, "bh.acc_smem": 1, "bh.eval_unroll": u})
                          for u in (1, 4)]
-    assert keys[6:] == [{"bh.walk": 1, "bh.group": 32, "bh.walk_blocks": b} for b in (6, 8)] + \
+    assert keys[4:6] == [dict(g64, **{"bh.walk_blocks": b, "bh.acc_smem": 0}) for b in (4, 5)]
+    assert keys[6:8] == [dict(g64, **{"bh.walk_blocks": 4, "bh.acc_smem": 0, "bh.eval_unroll": u})
+                         for u in (1, 4)]
+    assert keys[8:] == [{"bh.walk": 1, "bh.group": 32, "bh.walk_blocks": b} for b in (6, 8)] + \
         [{"bh.walk": 0}]
     assert e.tune_get("bh.walk") == rep["best"]["bh.walk"]
 
