@@ -613,29 +613,42 @@ bh_test_cap_kernel(int n, int stride, int samples, TreeState t, int stack_cap, u
     int sp = active ? 1 : 0;
     unsigned long long tests = 0, limit = 4096;
     for (int round = 0; round < 40; ++round, limit *= 2) {
+        // two node tests per lane and step (32 entries popped): the same
+        // tests as the walk in another order, with two loads in flight
         while (sp > 0 && tests <= limit) {
-            const int k = min(sp, 16);
-            int c = 0;
-            if (lane < 2 * k) c = 2 * stack[sp - 1 - (lane >> 1)] + (lane & 1);
+            const int k = min(sp, 32);
+            int c[2];
+            bool open[2];
+#pragma unroll
+            for (int w = 0; w < 2; ++w) {
+                const int slot = lane + 32 * w;
+                c[w] = slot < 2 * k ? 2 * stack[sp - 1 - (slot >> 1)] + (slot & 1) : 0;
+            }
             __syncwarp();
             sp -= k;
-            const bool valid = lane < 2 * k && c != 0;
-            bool open = false;
-            if (valid && c < n) {
-                const float4 nd = __ldg(&t.node4[c]);
-                const float ex = fmaxf(fabsf(nd.x - cb[0]) - hb[0], 0.f);
-                const float ey = fmaxf(fabsf(nd.y - cb[1]) - hb[1], 0.f);
-                const float ez = fmaxf(fabsf(nd.z - cb[2]) - hb[2], 0.f);
-                open = !(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > nd.w);
+            int nvalid = 0;
+#pragma unroll
+            for (int w = 0; w < 2; ++w) {
+                open[w] = false;
+                if (c[w] != 0 && c[w] < n) {
+                    const float4 nd = __ldg(&t.node4[c[w]]);
+                    const float ex = fmaxf(fabsf(nd.x - cb[0]) - hb[0], 0.f);
+                    const float ey = fmaxf(fabsf(nd.y - cb[1]) - hb[1], 0.f);
+                    const float ez = fmaxf(fabsf(nd.z - cb[2]) - hb[2], 0.f);
+                    open[w] = !(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > nd.w);
+                }
+                nvalid += __popc(__ballot_sync(0xffffffffu, c[w] != 0));
             }
-            tests += (unsigned long long)__popc(__ballot_sync(0xffffffffu, valid));
-            const unsigned om = __ballot_sync(0xffffffffu, open);
-            const int npush = __popc(om);
+            tests += (unsigned long long)nvalid;
+            const unsigned om0 = __ballot_sync(0xffffffffu, open[0]);
+            const unsigned om1 = __ballot_sync(0xffffffffu, open[1]);
+            const int npush = __popc(om0) + __popc(om1);
             if (sp + npush > stack_cap) {  // the walk itself reports the overflow
                 sp = 0;
                 break;
             }
-            if (open) stack[sp + __popc(om & lt)] = c;
+            if (open[0]) stack[sp + __popc(om0 & lt)] = c[0];
+            if (open[1]) stack[sp + __popc(om0) + __popc(om1 & lt)] = c[1];
             sp += npush;
             __syncwarp();
         }
