@@ -789,40 +789,53 @@ __global__ void quad_leaf_kernel(float4* quad, int n) {
     }
 }
 
-__global__ void quad_level_kernel(int first, TreeState t) {
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < first; k += gridDim.x * blockDim.x) {
-        const size_t idx = (size_t)first + k;
-        const float4 pc = t.node4[idx];
-        float xx = 0.f, yy = 0.f, zz = 0.f, xy = 0.f, xz = 0.f, yz = 0.f;
-        for (int side = 0; side < 2; ++side) {
-            const size_t c = 2 * idx + side;
-            const float4 cc = t.node4[c];
-            const float mc = t.nodem[c];
-            const float4 q0 = t.quad[2 * c], q1 = t.quad[2 * c + 1];
-            const float dx = cc.x - pc.x, dy = cc.y - pc.y, dz = cc.z - pc.z;
-            xx += q0.x + mc * dx * dx;
-            yy += q0.y + mc * dy * dy;
-            zz += q0.z + mc * dz * dz;
-            xy += q1.x + mc * dx * dy;
-            xz += q1.y + mc * dx * dz;
-            yz += q1.z + mc * dy * dz;
-        }
-        t.quad[2 * idx] = make_float4(xx, yy, zz, 0.5f * (xx + yy + zz));
-        t.quad[2 * idx + 1] = make_float4(xy, xz, yz, 0.f);
+__device__ __forceinline__ void quad_node(size_t idx, TreeState& t) {
+    const float4 pc = t.node4[idx];
+    float xx = 0.f, yy = 0.f, zz = 0.f, xy = 0.f, xz = 0.f, yz = 0.f;
+    for (int side = 0; side < 2; ++side) {
+        const size_t c = 2 * idx + side;
+        const float4 cc = t.node4[c];
+        const float mc = t.nodem[c];
+        const float4 q0 = t.quad[2 * c], q1 = t.quad[2 * c + 1];
+        const float dx = cc.x - pc.x, dy = cc.y - pc.y, dz = cc.z - pc.z;
+        xx += q0.x + mc * dx * dx;
+        yy += q0.y + mc * dy * dy;
+        zz += q0.z + mc * dz * dz;
+        xy += q1.x + mc * dx * dy;
+        xz += q1.y + mc * dx * dz;
+        yz += q1.z + mc * dy * dz;
+    }
+    t.quad[2 * idx] = make_float4(xx, yy, zz, 0.5f * (xx + yy + zz));
+    t.quad[2 * idx + 1] = make_float4(xy, xz, yz, 0.f);
+}
+
+// Levels [lv_lo, lv_hi) of the moments, bottom-up, in one launch: block b
+// owns the subtree under node 2^lv_lo + b (at most 9 levels, 256 nodes at
+// its bottom), a block barrier between levels.
+__global__ void __launch_bounds__(256) quad_levels_kernel(int lv_lo, int lv_hi, TreeState t) {
+    const size_t root = ((size_t)1 << lv_lo) + blockIdx.x;
+    for (int lv = lv_hi - 1; lv >= lv_lo; --lv) {
+        const int span = 1 << (lv - lv_lo);
+        const size_t first = root << (lv - lv_lo);
+        for (int k = threadIdx.x; k < span; k += blockDim.x) quad_node(first + k, t);
+        __syncthreads();
     }
 }
 
 nbg_status tree_quadrupoles(nbg_engine* e) {
     TreeState* t = e->tree;
-    if (t->quad == nullptr) NBG_CUDA(e, cudaMalloc(&t->quad, 2 * t->size * sizeof(float4)));
     const int n = (int)t->n;
-    quad_leaf_kernel<<<grid_for(n, 256, (unsigned)e->sm_count * 8u), 256, 0, e->stream>>>(t->quad, n);
-    NBG_LAUNCHED(e, "quad_leaf_kernel");
-    for (int lv = t->levels - 1; lv >= 0; --lv) {
-        const int first = 1 << lv;
-        quad_level_kernel<<<grid_for(first, 256, (unsigned)e->sm_count * 8u), 256, 0, e->stream>>>(
-            first, *t);
-        NBG_LAUNCHED(e, "quad_level_kernel");
+    if (t->quad == nullptr) {
+        NBG_CUDA(e, cudaMalloc(&t->quad, 2 * t->size * sizeof(float4)));
+        // leaves have no moments; only inner nodes are written afterwards
+        quad_leaf_kernel<<<grid_for(n, 256, (unsigned)e->sm_count * 8u), 256, 0, e->stream>>>(t->quad, n);
+        NBG_LAUNCHED(e, "quad_leaf_kernel");
+    }
+    for (int hi = t->levels; hi > 0;) {
+        const int lo = std::max(0, hi - 9);
+        quad_levels_kernel<<<1u << lo, 256, 0, e->stream>>>(lo, hi, *t);
+        NBG_LAUNCHED(e, "quad_levels_kernel");
+        hi = lo;
     }
     return NBG_OK;
 }
