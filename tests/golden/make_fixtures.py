@@ -3,7 +3,8 @@
 The reference (drons/nbody) pins its solvers with 16-body end states after
 t = 0.3 (test/solver/test_nbody_solver.cpp:43-145): the initial state
 test/data/initial_state.txt and one end state per solver, compared at 1e-12
-absolute.  The GPU machine has no copy of the reference, so the files travel with
+absolute.  Its data loaders are pinned with a Zeno ASCII snapshot, the same
+bodies as a table, and three malformed tables.  The GPU machine has no copy of the reference, so the files travel with
 the tests.  Run from the repository root:
 
     python tests/golden/make_fixtures.py /path/to/reference
@@ -15,7 +16,9 @@ from pathlib import Path
 FILES = ["initial_state", "euler", "rk4", "rkdp", "rkdp-corr", "rkck", "rkf",
          "midpoint", "rkdverk", "rkfeagin10", "rkfeagin12", "rkfeagin14",
          "rkgl", "rklc", "adams5", "adams5-corr", "bulirsch-stoer",
-         "midpoint-st", "rkfeagin10-corr", "trapeze2"]
+         "midpoint-st", "rkfeagin10-corr", "trapeze2",
+         # the loaders' fixtures (test/stream/test_nbody_stream.cpp:344-372)
+         "zeno_ascii", "zeno_table", "inv_column", "inv_columns_count", "inv_radius"]
 
 
 def main(ref_root: str) -> None:
