@@ -37,6 +37,10 @@ class NBodyData:
     time: float = 0.0
     step: int = 0
     box_size: int = 0
+    check_list: str = "PLVE"
+    _initial: dict = field(default=None, repr=False)
+    _last: dict = field(default=None, repr=False)
+    _prev_compute_count: int = field(default=0, repr=False)
 
     # -- nbody/nbody_data.cpp:176-212 ----------------------------------------
     def get_color(self) -> np.ndarray:
@@ -65,6 +69,61 @@ class NBodyData:
 
     def set_step(self, s: int) -> None:
         self.step = int(s)
+
+    # -- conservation check: nbody/nbody_data.cpp:57-145, 366-381 -------------
+    def set_check_list(self, check_list: str) -> None:
+        """Which of P, L, V, E print_statistics computes."""
+        self.check_list = check_list
+
+    def print_statistics(self, engine=None) -> str:
+        """The reference's conservation line: step, time, compute counts and
+        the drifts of momentum (dP, %), angular momentum (dL, %), mass-centre
+        speed (Vcm) and energy (dE, %) against the first call.  The sums are
+        the engine's FP64 GPU reductions of its current state (nbg_statistics)
+        instead of the reference's host sums after get_data; the bodies are
+        still fetched into this object, as the reference does.  Returns the
+        line (also printed)."""
+        cc = 0
+        if engine is not None:
+            engine.get_data(self)
+            cc = engine.get_compute_count()
+            st = engine.statistics()
+        else:
+            raise ValueError("print_statistics needs the engine that holds the state")
+        now = {"P": st[0:3].copy(), "L": st[3:6].copy(), "KE": float(st[6]),
+               "PE": float(st[7]), "V": st[8:11].copy()}
+        if self._initial is None:
+            self._initial = now
+        self._last = now
+        parts = [f"#{self.step:08d}", f"t {self.time:.6f}", f"CC {cc:08d}",
+                 f"SC {cc - self._prev_compute_count:8d}"]
+        self._prev_compute_count = cc
+        if "P" in self.check_list:
+            parts.append(f"dP {self.get_impulce_err():.3e}")
+        if "L" in self.check_list:
+            parts.append(f"dL {self.get_impulce_moment_err():.3e}")
+        if "V" in self.check_list:
+            vcm = (self._last["V"] - self._initial["V"]) / self.time if self.time else \
+                np.zeros(3)
+            parts.append(f"Vcm {np.linalg.norm(vcm):.3e}")
+        if "E" in self.check_list:
+            parts.append(f"dE {self.get_energy_err():.3e}")
+        line = " ".join(parts)
+        print(line)
+        return line
+
+    def get_impulce_err(self) -> float:
+        p0, p1 = self._initial["P"], self._last["P"]
+        return abs(100.0 * np.linalg.norm(p1 - p0) / np.linalg.norm(p0))
+
+    def get_impulce_moment_err(self) -> float:
+        l0, l1 = self._initial["L"], self._last["L"]
+        return abs(100.0 * np.linalg.norm(l1 - l0) / np.linalg.norm(l0))
+
+    def get_energy_err(self) -> float:
+        e0 = self._initial["KE"] + self._initial["PE"]
+        e1 = self._last["KE"] + self._last["PE"]
+        return abs(100.0 * (e1 - e0) / e0)
 
     # -- state vector helpers --------------------------------------------------
     def to_state(self) -> np.ndarray:

@@ -30,3 +30,32 @@ def test_statistics_match_oracle(make_engine, oracle, case):
     err = np.abs(got - ref) / np.maximum(scale, np.abs(ref[8:11]).max() * (np.arange(12) >= 8))
     print(f"\n{case}: max rel {err.max():.2e}")
     assert np.all(np.abs(got - ref) <= 1e-12 * np.maximum(scale, 1e-12) + 1e-15)
+
+
+def test_print_statistics_tracks_drift(make_engine, oracle):
+    """nbody_data::print_statistics with the engine's GPU sums: the first
+    call fixes the initial values (zero drift), later calls report the
+    percent drifts of P, L and E against them, equal to the same drifts
+    from the oracle's host sums of the states get_data returns."""
+    from nbody_gb300.solvers import create_solver
+    d = NBodyData.load(str(GOLDEN / "initial_state.txt"))
+    e = make_engine(precision="fp64")
+    assert e.init(d)
+    s = create_solver({"solver": "rk4"})
+    s.set_engine(e)
+    s.set_time_step(1e-2, 1e-2)
+    line0 = d.print_statistics(e)
+    assert "dP 0.000e+00" in line0 and "dE 0.000e+00" in line0 and line0.startswith("#00000000")
+    st0 = oracle.statistics(d.to_state(), d.mass)
+    for _ in range(20):
+        s.advise(1e-2)
+    line = d.print_statistics(e)
+    st1 = oracle.statistics(d.to_state(), d.mass)
+    e0, e1 = st0[6] + st0[7], st1[6] + st1[7]
+    de = abs(100.0 * (e1 - e0) / e0)
+    dp = abs(100.0 * np.linalg.norm(st1[0:3] - st0[0:3]) / np.linalg.norm(st0[0:3]))
+    print("\n" + line)
+    assert d.get_step() == 20 and abs(d.get_time() - 0.2) < 1e-12
+    assert abs(d.get_energy_err() - de) <= 1e-9 * max(de, 1e-3)
+    assert abs(d.get_impulce_err() - dp) <= 1e-6 * max(dp, 1e-6) + 1e-12
+    assert f"dE {d.get_energy_err():.3e}" in line
