@@ -341,11 +341,14 @@ def accuracy_frontier(n_bh: int, rows, a_ref, d, targets=(1e-2, 1e-3, 1e-4)):
     reference's own method) and with quadrupole cells, and the direct sum."""
     from nbody_gb300.engine import create_engine
     tightest = min(targets)
+    # opening ratios in steps of about 10 % (the error changes by about 25 %
+    # per step), the same grid density for every family
+    grid = [round(1.0 * 1.1 ** k, 3) for k in range(0, 42)]  # 1.0 .. 50
     families = (
-        (2, 2, (1.0, 1.2, 1.5, 2.0, 2.5, 3.0, 3.5, 4.0, 4.5, 5.0, 6.0)),
-        (2, 1, (1.5, 2.0, 2.5, 3.0, 4.0, 6.0, 8.0, 12.0, 16.0, 24.0, 32.0)),
-        (0, 1, (1.0 / 0.9, 2.0, 3.0, 4.0, 6.0, 8.0, 12.0, 16.0, 24.0, 32.0, 48.0)),
-        (0, 2, (2.0, 3.0, 3.5, 4.0, 5.0, 6.0)),
+        (2, 2, grid),
+        (2, 1, [g for g in grid if g >= 1.5]),
+        (0, 1, [g for g in grid if g >= 1.1]),
+        (0, 2, [g for g in grid if g >= 1.5]),
     )
     cands = []
     for build, order, lams in families:
