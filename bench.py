@@ -235,13 +235,15 @@ def read_traffic():
 
 
 def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 5, walk: int = 1,
-             weights=None, order: int = 1, build_rate: int = 0, build: int = 2):
+             weights=None, order: int = 1, build_rate: int = 0, build: int = 2,
+             precision: str = "mixed"):
     """Barnes-Hut fcompute (tree rebuilt every call) at opening ratio lam.
     walk 1 = group walk with interaction lists, 0 = warp-coherent stackless;
-    build 0 = the reference's kd-median tree, 1 Morton, 2 Hilbert order."""
+    build 0 = the reference's kd-median tree, 1 Morton, 2 Hilbert order;
+    precision "fp64" = the reference's per-body walk and arithmetic."""
     from nbody_gb300 import _lib
     from nbody_gb300.engine import create_engine
-    e = create_engine({"engine": "gb300", "algo": "bh", "precision": "mixed",
+    e = create_engine({"engine": "gb300", "algo": "bh", "precision": precision,
                        "softening": SOFTENING, "distance_to_node_radius_ratio": lam,
                        "learned": learned, "tree_layout": "heap_stackless",
                        "tree_build_rate": build_rate})
@@ -282,8 +284,10 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
     # node records read by the walk (20 B each: com.xyz + crit^2, mass), per
     # warp test, plus the body rows (16 B in, 24 B out)
     walk_bytes = visits / calls * 20.0 + n_bh * 40.0
+    if precision == "fp64":
+        build, walk = 0, -1  # always the reference's tree and per-body walk
     return {"lambda": lam, "theta": 1.0 / lam, "walk": walk, "learned": learned, "order": order,
-            "build": ("kd-median", "morton", "hilbert")[build],
+            "precision": precision, "build": ("kd-median", "morton", "hilbert")[build],
             "bodies_per_s": n_bh / (ms * 1e-3),
             "walk_node_gbs": walk_bytes / (tw / max(nw, 1) * 1e-3) / 1e9,
             "ms_per_fcompute": ms, "wall_ms_per_fcompute": wall * 1e3,
@@ -446,6 +450,9 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
                                                          order=2),
         "coherent_walk_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, walk=0,
                                                     build=0),
+        # the FP64 parity path: the reference's tree, walk and arithmetic
+        "fp64_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, calls=1,
+                                           precision="fp64"),
         "coherent_walk_hilbert_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d,
                                                             walk=0),
         # tree_build_rate 4 (the reference's refit option): one build and
