@@ -113,6 +113,24 @@ def test_bh_mixed_error_vs_direct(make_engine, oracle, lam, walk):
     assert np.median(rel) <= np.median(rel_ref)
 
 
+@pytest.mark.parametrize("n", [1, 2, 8, 16])
+def test_bh_mixed_tiny(make_engine, oracle, n):
+    """Below one warp group the mixed path walks per body (on the default
+    Hilbert tree); at lambda 1e8 every node opens and the forces are the
+    direct sum's."""
+    d = NBodyData.plummer(n, seed=n + 3)
+    y = d.to_state()
+    e = make_engine(algo="bh", precision="mixed", softening=1e-3,
+                    distance_to_node_radius_ratio=1e8)
+    assert e.init(d)
+    f = _f(e, y)
+    assert np.array_equal(f[:3 * n], y[3 * n:])
+    a_ref = oracle.accel_rows(y, d.mass, 1e-3, rows=np.arange(n))
+    a = f[3 * n:].reshape(3, n).T
+    scale = max(np.abs(a_ref).max(), 1e-30)
+    assert np.all(np.abs(a - a_ref) <= 1e-5 * scale)
+
+
 @pytest.mark.parametrize("n", [32, 64, 1024])
 def test_bh_group_walk_small(make_engine, oracle, n):
     """Group walk on one or a few warps.  One warp (n = 32) opens the whole
