@@ -391,9 +391,10 @@ def accuracy_frontier(n_bh: int, rows, a_ref, d, targets=(1e-2, 1e-3, 1e-4)):
     return {"targets_p99": list(targets), "best": best, "candidates": cands}
 
 
-def train_correction(epochs: int = 8):
-    """Samples from two snapshots the timed one is not (Plummer and uniform
-    cube, N = 2^16), trained on the GPU; returns the weights and the fit."""
+def train_correction(epochs: int = 8, samples: int = 20_000_000):
+    """About 2e7 exact-subtree samples from Plummer and uniform-cube snapshots
+    with N in {2^16, 2^18, 2^20}, none of them the timed one, trained on the
+    GPU; returns the weights and the fit."""
     from nbody_gb300.data import NBodyData
     from nbody_gb300.engine import create_engine
     e = create_engine({"engine": "gb300", "algo": "bh", "precision": "mixed",
@@ -401,10 +402,13 @@ def train_correction(epochs: int = 8):
                        "learned_tight_ratio": 2.0})
     t0 = time.perf_counter()
     total = 0
-    for i, d in enumerate((NBodyData.plummer(1 << 16, seed=41),
-                           NBodyData.uniform_cube(1 << 16, side=2.0, seed=42))):
-        e.init(d)
-        total += e.learn_generate(500000, seed=50 + i)
+    snaps = [(k, i) for i, k in enumerate((16, 18, 20))]
+    for j, (k, i) in enumerate(snaps):
+        for kind in ("plummer", "cube"):
+            d = NBodyData.plummer(1 << k, seed=41 + 2 * i) if kind == "plummer" else \
+                NBodyData.uniform_cube(1 << k, side=2.0, seed=42 + 2 * i)
+            e.init(d)
+            total += e.learn_generate(samples // (2 * len(snaps)), seed=50 + 2 * j + (kind == "cube"))
     gen_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     tr, va = e.learn_train(epochs, batch=8192, lr=3e-3, seed=5)
@@ -455,6 +459,9 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
                                            precision="fp64"),
         "coherent_walk_hilbert_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d,
                                                             walk=0),
+        # the walk the learned correction extends, without it
+        "coherent_walk_theta_0.9": lambda: bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d,
+                                                    walk=0, build=0),
         # tree_build_rate 4 (the reference's refit option): one build and
         # three refits per four fcomputes; same positions, so the same forces
         "refit_rate4_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, calls=8,
@@ -490,7 +497,8 @@ def bh_summary(bh):
                                         "bodies_per_s": b["bodies_per_s"],
                                         "speedup_vs_reference_method":
                                             b["speedup_vs_reference_method"]}
-    for k in ("hilbert_theta_0.5", "plain_theta_0.5", "learned_theta_0.9"):
+    for k in ("hilbert_theta_0.5", "plain_theta_0.5", "learned_theta_0.9",
+              "coherent_walk_theta_0.9"):
         if k in bh:
             out[k] = {x: bh[k][x] for x in ("ms_per_fcompute", "bodies_per_s", "p50", "p99")}
     return out
