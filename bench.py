@@ -236,7 +236,7 @@ def read_traffic():
 
 def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 5, walk: int = 1,
              weights=None, order: int = 1, build_rate: int = 0, build: int = 2,
-             precision: str = "mixed"):
+             precision: str = "mixed", tune=None):
     """Barnes-Hut fcompute (tree rebuilt every call) at opening ratio lam.
     walk 1 = group walk with interaction lists, 0 = warp-coherent stackless;
     build 0 = the reference's kd-median tree, 1 Morton, 2 Hilbert order;
@@ -252,6 +252,8 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
     e.tune_set("bh.walk", walk)
     e.tune_set("bh.order", order)
     e.tune_set("bh.build", build)
+    for k, v in (tune or {}).items():
+        e.tune_set(k, v)
     if not e.init(d):
         return {"unavailable": "engine init failed"}
     if weights is not None:
@@ -434,7 +436,7 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
 
     def learned_case():
         w, fit = train_correction()
-        r = bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=w, build=0)
+        r = bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=w)
         r["training"] = fit
         return r
 
@@ -459,9 +461,10 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
                                            precision="fp64"),
         "coherent_walk_hilbert_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d,
                                                             walk=0),
-        # the walk the learned correction extends, without it
+        # the walk the learned correction extends (with its FP64 node
+        # update), without the correction
         "coherent_walk_theta_0.9": lambda: bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d,
-                                                    walk=0, build=0),
+                                                    walk=0, tune={"bh.fp64_nodes": 1}),
         # tree_build_rate 4 (the reference's refit option): one build and
         # three refits per four fcomputes; same positions, so the same forces
         "refit_rate4_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, calls=8,
@@ -475,11 +478,14 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
     for name, run in suite.items():
         if cases is None or name in cases:
             res[name] = run()
-    if "plain_theta_0.5" in res and "learned_theta_0.9" in res:
-        p05, l09 = res["plain_theta_0.5"], res["learned_theta_0.9"]
-        res["learned_0.9_vs_plain_0.5"] = {
-            "bodies_per_s_ratio": l09["bodies_per_s"] / p05["bodies_per_s"],
-            "p99_ratio": l09["p99"] / p05["p99"]}
+    # the learned walk against plain theta 0.5 on the same GPU: the default
+    # (Hilbert tree, group walk) and the reference's tree
+    for base in ("hilbert_theta_0.5", "plain_theta_0.5"):
+        if base in res and "learned_theta_0.9" in res:
+            p05, l09 = res[base], res["learned_theta_0.9"]
+            res[f"learned_0.9_vs_{base}"] = {
+                "bodies_per_s_ratio": l09["bodies_per_s"] / p05["bodies_per_s"],
+                "p99_ratio": l09["p99"] / p05["p99"]}
     return res
 
 

@@ -249,8 +249,7 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       "bh.group" (64 or 32 bodies per warp in the group walk),
  *       "bh.build" (0: the reference's kd-median tree, always for FP64;
  *       mixed precision: 1 leaves in Morton order, 2 in Hilbert order (the
- *       default, except for the learned correction's walk and its training
- *       samples, which use the kd tree), every node the two halves of its range -- one sort
+ *       default), every node the two halves of its range -- one sort
  *       instead of three, a different tree with compact cells),
  *       "bh.fp64_nodes" (mixed precision: 1 forms the FP64 node arrays as
  *       the FP64 path does; default 0, only the FP32 records the mixed walks

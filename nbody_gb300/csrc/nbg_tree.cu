@@ -659,12 +659,10 @@ nbg_status tree_build(nbg_engine* e, const double* y, bool fp64_nodes) {
     ProfScope ps(e, NBG_K_TREE_BUILD);
     const unsigned g = grid_for(n, 256, (unsigned)e->sm_count * 8u);
     // mixed precision defaults to the Hilbert tree: at equal force error
-    // its group walk does several times fewer node tests than on the kd
-    // tree, whose median cuts leave long thin cells with large radii.  The
-    // builds that need FP64 nodes (the FP64 walk; the learned correction's
-    // walk and its training samples, which are made and measured on the kd
-    // tree) keep the reference's tree.
-    const bool hilbert_default = !fp64_nodes;
+    // its walks do several times fewer node tests than on the kd tree,
+    // whose median cuts leave long thin cells with large radii.  The FP64
+    // path keeps the reference's tree.
+    const bool hilbert_default = e->params.precision != NBG_PREC_FP64;
     const int64_t curve = e->tune_get("bh.build", hilbert_default ? 2 : 0);
     if (e->params.precision != NBG_PREC_FP64 && (curve == 1 || curve == 2)) {
         // space-filling-curve order (1: Morton, 2: Hilbert): one sort; leaf p

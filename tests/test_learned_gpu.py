@@ -103,15 +103,18 @@ def test_samples_match_cpu_recomputation(make_engine):
         assert lam * s < dist * (1 + 1e-4) and dist <= 2.0 * s * (1 + 1e-4)
 
 
-def _trained_weights(make_engine, epochs=20):
+def _trained_weights(make_engine, epochs=8):
+    """About 6e6 samples from Plummer and uniform-cube snapshots of 2^14 to
+    2^18 bodies (the generalisation needs many snapshots and sizes)."""
     e = _bh_engine(make_engine, 1.0 / 0.9)
     total = 0
-    for i, (n, kind) in enumerate(((1 << 14, "plummer"), (1 << 15, "cube"), (1 << 16, "plummer"))):
+    sizes = [(1 << k, kind) for k in (14, 16, 18) for kind in ("plummer", "cube")]
+    for i, (n, kind) in enumerate(sizes):
         d = NBodyData.plummer(n, seed=10 + i) if kind == "plummer" else \
             NBodyData.uniform_cube(n, side=2.0, seed=10 + i)
         assert e.init(d)
-        total += e.learn_generate(400000, seed=20 + i)
-    x, t, _ = e.learn_read_samples(0, total)
+        total += e.learn_generate(1_000_000, seed=20 + i)
+    x, t, _ = e.learn_read_samples(0, min(total, 200000))
     var0 = float((t[:, :3].astype(np.float64) ** 2).mean())
     tr, va = e.learn_train(epochs, batch=8192, lr=3e-3, seed=5)
     print(f"\nsamples {total}, target mean square {var0:.3e}, train MSE {tr:.3e}, val MSE {va:.3e}")
@@ -176,9 +179,8 @@ def test_learned_walk_vs_plain(make_engine, oracle, trained, group):
 
     def run(lam, learned):
         e = _bh_engine(make_engine, lam, learned=learned)
-        e.tune_set("bh.walk", 0)  # the walk the learned path extends
-        e.tune_set("bh.build", 0)  # on the kd tree the learned path keeps,
-        e.tune_set("bh.fp64_nodes", 1)  # with its FP64 node update
+        e.tune_set("bh.walk", 0)  # the walk the learned path extends,
+        e.tune_set("bh.fp64_nodes", 1)  # with the FP64 node update it uses
         assert e.init(d)
         if learned:
             e.learn_set_weights(w)
