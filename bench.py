@@ -15,6 +15,15 @@ of rows of the same workload; it runs on rank 0 only.
 
 Multi-GPU: the path is run as independent replicas (one per rank); value is
 the sum over ranks of the pairs processed divided by the slowest rank's time.
+
+Rank 0 also runs, outside the timed region, and adds to the same line:
+  bh          the Barnes-Hut suite at N = 2^20 (both trees, monopole and
+              quadrupole cells, the coherent and the FP64 walks, refit, the
+              learned correction, the accuracy frontier, the rkdp run);
+  bh_summary  the suite's figures of the headline metric;
+  ensemble    2048 Plummer clusters stepped by the device-side rkdp;
+  statistics  P, L, E, V of one state on the GPU against the host sums.
+    python bench.py --bh-only [--bh-n N] [--bh-cases a,b]   the suite alone
 """
 from __future__ import annotations
 
