@@ -336,9 +336,11 @@ nbg_status nbg_ensemble_fcompute(nbg_ensemble* s, double* f);
  * potential of the ensemble's softening). */
 nbg_status nbg_ensemble_statistics(nbg_ensemble* s, double* out);
 /* Tuning keys "ensemble.pairs_per_lane" (1 or 2: i-tile of 256 or 512 bodies
- * per work unit), "ensemble.blocks_per_sm" (0 = as many as fit) and
- * "ensemble.unroll" (2, 4 or 8: j-loop unroll of the force kernel); a change
- * takes effect from the next step (the step graph is captured again). */
+ * per work unit), "ensemble.blocks_per_sm" (0 = as many as fit),
+ * "ensemble.unroll" (2, 4 or 8: j-loop unroll of the force kernel) and
+ * "ensemble.hold_after_reject" (1, the default: a system's step may not grow
+ * right after a rejected step; 0: it may, up to 5x); a change takes effect
+ * from the next step (the step graph is captured again). */
 nbg_status nbg_ensemble_tune_set(nbg_ensemble* s, const char* key, int64_t value);
 /* Autotuner of the ensemble force kernel (tile shape and grid), timed on the
  * current state; keeps the fastest; JSON report as nbg_autotune. */

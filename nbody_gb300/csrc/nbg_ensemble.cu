@@ -237,15 +237,19 @@ __global__ void ens_error_kernel(const double* __restrict__ y, const int* __rest
 }
 
 // One thread per system: accept / reject and the next step.
+// hold: after a rejected step the next step may not grow (Hairer, Norsett &
+// Wanner, Solving ODEs I, sec. II.4), which avoids reject / grow cycles.
 __global__ void ens_control_kernel(int nsys, double tol, double dt_min, double dt_max,
                                    const unsigned long long* __restrict__ err, double* __restrict__ dt,
                                    double* __restrict__ t, unsigned* __restrict__ accepted,
-                                   unsigned* __restrict__ rejected, int* __restrict__ decision) {
+                                   unsigned* __restrict__ rejected, int* __restrict__ decision,
+                                   int hold) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nsys) return;
     const double e = __longlong_as_double((long long)err[s]);
     const double h = dt[s];
     const bool ok = e <= tol || h <= dt_min;
+    const bool after_reject = decision[s] == 0;
     decision[s] = ok ? 1 : 0;
     if (ok) {
         t[s] += h;
@@ -254,7 +258,7 @@ __global__ void ens_control_kernel(int nsys, double tol, double dt_min, double d
         rejected[s] += 1;
     }
     double fac = (e > 0.0) ? 0.9 * pow(tol / e, 0.2) : 5.0;
-    fac = fmin(5.0, fmax(0.2, fac));
+    fac = fmin((hold && after_reject) ? 1.0 : 5.0, fmax(0.2, fac));
     dt[s] = fmin(dt_max, fmax(dt_min, h * fac));
 }
 
@@ -398,7 +402,7 @@ nbg_status ens_enqueue_step(nbg_ensemble* s) {
     NBG_LAUNCHED(e, "ens_error_kernel");
     ens_control_kernel<<<(s->nsys + 127) / 128, 128, 0, e->stream>>>(
         s->nsys, s->p.tolerance, s->p.dt_min, s->p.dt_max, s->err, s->dt, s->t, s->accepted,
-        s->rejected, s->decision);
+        s->rejected, s->decision, (int)e->tune_get("ensemble.hold_after_reject", 1));
     NBG_LAUNCHED(e, "ens_control_kernel");
     ens_commit_kernel<<<gv, 256, 0, e->stream>>>(s->y, s->ynew, s->sys, s->decision, s->B);
     NBG_LAUNCHED(e, "ens_commit_kernel");
@@ -533,6 +537,8 @@ nbg_status nbg_ensemble_init(nbg_ensemble* s, size_t nsys, const uint32_t* count
     NBG_CUDA(e, cudaMemcpy(s->t, t0.data(), nsys * sizeof(double), cudaMemcpyHostToDevice));
     NBG_CUDA(e, cudaMemset(s->accepted, 0, nsys * sizeof(unsigned)));
     NBG_CUDA(e, cudaMemset(s->rejected, 0, nsys * sizeof(unsigned)));
+    const std::vector<int> ok0(nsys, 1);  // no step rejected yet
+    NBG_CUDA(e, cudaMemcpy(s->decision, ok0.data(), nsys * sizeof(int), cudaMemcpyHostToDevice));
     return ens_configure(s);
 }
 
