@@ -339,8 +339,11 @@ nbg_status nbg_ensemble_statistics(nbg_ensemble* s, double* out);
  * per work unit), "ensemble.blocks_per_sm" (0 = as many as fit),
  * "ensemble.unroll" (2, 4 or 8: j-loop unroll of the force kernel) and
  * "ensemble.hold_after_reject" (1, the default: a system's step may not grow
- * right after a rejected step; 0: it may, up to 5x); a change takes effect
- * from the next step (the step graph is captured again). */
+ * right after a rejected step; 0: it may, up to 5x) and
+ * "ensemble.pi_control" (1: PI step control on accepted steps, fewer
+ * rejections and smaller steps; 0, the default: the error of the current
+ * step only); a change takes effect from the next step (the step graph is
+ * captured again). */
 nbg_status nbg_ensemble_tune_set(nbg_ensemble* s, const char* key, int64_t value);
 /* Autotuner of the ensemble force kernel (tile shape and grid), timed on the
  * current state; keeps the fastest; JSON report as nbg_autotune. */

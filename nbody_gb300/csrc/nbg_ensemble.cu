@@ -243,7 +243,7 @@ __global__ void ens_control_kernel(int nsys, double tol, double dt_min, double d
                                    const unsigned long long* __restrict__ err, double* __restrict__ dt,
                                    double* __restrict__ t, unsigned* __restrict__ accepted,
                                    unsigned* __restrict__ rejected, int* __restrict__ decision,
-                                   int hold) {
+                                   int hold, double* __restrict__ err_prev, int pi) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nsys) return;
     const double e = __longlong_as_double((long long)err[s]);
@@ -257,7 +257,16 @@ __global__ void ens_control_kernel(int nsys, double tol, double dt_min, double d
     } else {
         rejected[s] += 1;
     }
-    double fac = (e > 0.0) ? 0.9 * pow(tol / e, 0.2) : 5.0;
+    double fac;
+    if (pi && ok && e > 0.0) {
+        // PI step control (Gustafsson 1991): exponents 0.7/5 on this error
+        // and 0.4/5 on the previous accepted step's
+        const double ep = fmax(err_prev[s], 1e-4 * tol);
+        fac = 0.9 * pow(tol / e, 0.14) * pow(ep / tol, 0.08);
+        err_prev[s] = e;
+    } else {
+        fac = (e > 0.0) ? 0.9 * pow(tol / e, 0.2) : 5.0;
+    }
     fac = fmin((hold && after_reject) ? 1.0 : 5.0, fmax(0.2, fac));
     dt[s] = fmin(dt_max, fmax(dt_min, h * fac));
 }
@@ -299,6 +308,7 @@ struct nbg_ensemble {
     unsigned* accepted = nullptr;
     unsigned* rejected = nullptr;
     int* decision = nullptr;
+    double* err_prev = nullptr;  // error of each system's last accepted step (PI control)
     EnsUnit* units = nullptr;
     int nunits = 0;
     unsigned* counters = nullptr;  // one per stage
@@ -402,7 +412,8 @@ nbg_status ens_enqueue_step(nbg_ensemble* s) {
     NBG_LAUNCHED(e, "ens_error_kernel");
     ens_control_kernel<<<(s->nsys + 127) / 128, 128, 0, e->stream>>>(
         s->nsys, s->p.tolerance, s->p.dt_min, s->p.dt_max, s->err, s->dt, s->t, s->accepted,
-        s->rejected, s->decision, (int)e->tune_get("ensemble.hold_after_reject", 1));
+        s->rejected, s->decision, (int)e->tune_get("ensemble.hold_after_reject", 1), s->err_prev,
+        (int)e->tune_get("ensemble.pi_control", 0));
     NBG_LAUNCHED(e, "ens_control_kernel");
     ens_commit_kernel<<<gv, 256, 0, e->stream>>>(s->y, s->ynew, s->sys, s->decision, s->B);
     NBG_LAUNCHED(e, "ens_commit_kernel");
@@ -411,7 +422,8 @@ nbg_status ens_enqueue_step(nbg_ensemble* s) {
 
 void ens_free(nbg_ensemble* s) {
     void* ptrs[] = {s->off, s->cnt, s->sys, s->y, s->ynew, s->mass, s->bodies, s->dt, s->t,
-                    s->err, s->accepted, s->rejected, s->decision, s->units, s->counters};
+                    s->err, s->accepted, s->rejected, s->decision, s->err_prev, s->units,
+                    s->counters};
     for (void* p : ptrs) cudaFree(p);
     for (double* k : s->k) cudaFree(k);
     if (s->graph) cudaGraphExecDestroy(s->graph);
@@ -516,6 +528,7 @@ nbg_status nbg_ensemble_init(nbg_ensemble* s, size_t nsys, const uint32_t* count
     NBG_CUDA(e, cudaMalloc(&s->accepted, nsys * sizeof(unsigned)));
     NBG_CUDA(e, cudaMalloc(&s->rejected, nsys * sizeof(unsigned)));
     NBG_CUDA(e, cudaMalloc(&s->decision, nsys * sizeof(int)));
+    NBG_CUDA(e, cudaMalloc(&s->err_prev, nsys * sizeof(double)));
     NBG_CUDA(e, cudaMalloc(&s->counters, kStagesRK * sizeof(unsigned)));
     // host-side layout: SoA state, system ids, LPT-ordered work units
     std::vector<double> h(B6);
@@ -539,6 +552,8 @@ nbg_status nbg_ensemble_init(nbg_ensemble* s, size_t nsys, const uint32_t* count
     NBG_CUDA(e, cudaMemset(s->rejected, 0, nsys * sizeof(unsigned)));
     const std::vector<int> ok0(nsys, 1);  // no step rejected yet
     NBG_CUDA(e, cudaMemcpy(s->decision, ok0.data(), nsys * sizeof(int), cudaMemcpyHostToDevice));
+    const std::vector<double> tol0(nsys, s->p.tolerance);  // PI control starts as the I control
+    NBG_CUDA(e, cudaMemcpy(s->err_prev, tol0.data(), nsys * sizeof(double), cudaMemcpyHostToDevice));
     return ens_configure(s);
 }
 
