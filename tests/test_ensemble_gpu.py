@@ -111,6 +111,33 @@ def test_adaptive_energy_drift(gpulib, oracle):
     ens.close()
 
 
+def test_step_control_variants(gpulib):
+    """The three step controllers on the same systems: without the hold
+    after a rejection, with it (the default), and PI control; each keeps the
+    energy drift small and PI control rejects fewer steps."""
+    rng = np.random.default_rng(5)
+    sizes = rng.integers(64, 1025, size=32).tolist()
+    sy = _systems(sizes, seed=13)
+    res = {}
+    for name, hold, pi in (("free", 0, 0), ("hold", 1, 0), ("pi", 1, 1)):
+        ens = Ensemble(tolerance=1e-8)
+        ens.tune_set("ensemble.hold_after_reject", hold)
+        ens.tune_set("ensemble.pi_control", pi)
+        ens.init(sy)
+        st0 = ens.statistics()
+        ens.step(30)
+        st1 = ens.statistics()
+        t, dt, acc, rej = ens.status()
+        e0, e1 = st0[:, 6] + st0[:, 7], st1[:, 6] + st1[:, 7]
+        res[name] = (acc.sum(), rej.sum(), float(np.abs((e1 - e0) / e0).max()), float(t.sum()))
+        ens.close()
+    print("\n" + "; ".join(f"{k}: accepted {a} rejected {r} drift {d:.1e} sum t {tt:.3f}"
+                           for k, (a, r, d, tt) in res.items()))
+    for a, r, d, _ in res.values():
+        assert a + r == 30 * 32 and d < 1e-5
+    assert res["pi"][1] < res["hold"][1]
+
+
 def test_ensemble_statistics_unsoftened_match_oracle(gpulib, oracle):
     sy = _systems([64, 500, 1200], seed=13)
     ens = Ensemble(softening=0.0)
