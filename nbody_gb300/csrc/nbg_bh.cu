@@ -21,9 +21,14 @@
 //    at least as accurate as the per-body walk at the same opening ratio.
 //    This walk is the one the learned correction extends (bh.walk = 0).
 //  * group walk (precision mixed, the default, bh.walk = 1): a warp tests 32
-//    nodes at a time against the bounding box of its 32 bodies and evaluates
-//    the accepted nodes from an interaction list in shared memory with packed
-//    FP32x2 pair math (details at bh_group_walk_kernel).
+//    nodes at a time against the bounding box of its 64 (or 32) bodies and
+//    evaluates the accepted nodes from an interaction list in shared memory
+//    with packed FP32x2 pair math (details at bh_group_walk_kernel).  Warps
+//    are persistent; a group that exceeds a node-test cap (bh_test_cap_kernel,
+//    from sampled groups' tests) is queued, and bh_body_walk_kernel walks its
+//    bodies one warp per body.
+//  * the quadrupole term (bh.order = 2) uses per-node second moments
+//    (quad_levels_kernel) in both the group walk and the per-body walk.
 #include <algorithm>
 
 #include "nbg_ptx.cuh"

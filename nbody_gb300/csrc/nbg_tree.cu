@@ -1,4 +1,6 @@
-// nbg_tree.cu -- GPU build of the reference's kd-median heap.
+// nbg_tree.cu -- GPU builds of the Barnes-Hut heap: the reference's
+// kd-median tree (always for FP64) and, for mixed precision, a tree whose
+// leaves follow a space-filling curve (Hilbert by default, or Morton).
 //
 // The reference builds the tree on the host (nbody/nbody_space_heap.cpp:13-37,
 // 136-190): recursive median split with std::nth_element along x, y, z in
@@ -15,11 +17,17 @@
 //     them; the two other lists are stably partitioned by that flag, which
 //     keeps every child segment ordered along all three axes.  After K levels
 //     the lists give the leaf order: leaf N + p holds body list[p].
-//  3. Bottom-up, one launch per level, the reference's node update in FP64
+//  3. Bottom-up, nine levels per launch, the reference's node update in FP64
 //     with explicit roundings (no contraction), so nodes match a
 //     non-contracting build of the reference bit for bit.
 // With distinct coordinates the subsets equal nth_element's; the whole tree,
 // and therefore every acceptance decision of the walk, matches the reference.
+//
+// Curve form: the bounding box, one 63-bit key per body (Morton, or the
+// Hilbert index by Skilling's transform), one stable radix sort of the key
+// bits from 16 up, leaf p = the p-th body along the curve, every node the
+// union of its two halves; mixed precision updates the nodes in FP32 from
+// FP32 boxes when no FP64 node arrays are needed.
 #include <algorithm>
 #include <cstring>
 
