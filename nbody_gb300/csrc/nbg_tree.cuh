@@ -27,7 +27,7 @@ struct TreeState {
     int* tile_count = nullptr;               // [2][n / kPartTile + 1]
     unsigned* hist = nullptr;                // radix per-block digit counts
     unsigned* totals = nullptr;              // radix per-digit totals
-    unsigned long long* box = nullptr;       // [6] order keys of the bounding box (Morton build)
+    unsigned long long* box = nullptr;       // [6] order keys of the bounding box (curve builds)
 
     // heap arrays, FP64 SoA (the reference's node fields)
     double* com = nullptr;    // [3][size] mass centre
@@ -69,9 +69,10 @@ struct TreeState {
 
 constexpr int kPartTile = 2048;  // elements per partition tile (256 threads x 8)
 
-// Full build.  Default: the reference's kd-median tree.  With the tuning key
-// "bh.build" = 1 and mixed precision: leaves in Morton order, the list
-// halved at every level (one sort, no partitions; a different tree).
+// Full build.  FP64 precision: the reference's kd-median tree.  Mixed
+// precision: leaves in Hilbert order ("bh.build" = 2, the default), Morton
+// order (1) or the kd-median tree (0); a curve tree halves the ordered list
+// at every level (one sort, no partitions; a different tree).
 // fp64_nodes: form the FP64 node arrays (the FP64 walk, the learned
 // correction's features); otherwise only the FP32 records
 nbg_status tree_build(nbg_engine* e, const double* y, bool fp64_nodes);
