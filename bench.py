@@ -483,6 +483,9 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
                                                  build=0),
         "quadrupole_hilbert_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d,
                                                          order=2),
+        # near the p99 <= 1e-4 point of the accuracy frontier
+        "quadrupole_hilbert_lambda_4": lambda: bench_bh(n_bh, 4.0, False, rows, a_ref, d,
+                                                        order=2),
         "coherent_walk_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, walk=0,
                                                     build=0),
         # the FP64 parity path: the reference's tree, walk and arithmetic
