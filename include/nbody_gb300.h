@@ -256,14 +256,16 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       read, from FP32 bounding boxes),
  *       "bh.test_cap" (node tests after which a group walk hands its bodies
  *       to the per-body walk; 0, the default, is "bh.test_cap_ratio"
- *       (default 3) times the previous walk's mean per group),
+ *       (default 2) times the median tests of 32 sampled groups of the
+ *       current tree; curve trees only, the kd tree is not capped),
  *       "bh.order" (1: monopole cells as the reference; 2: accepted cells
  *       add their quadrupole term, from FP32 second moments per node),
  *       "bh.walk_blocks" (4, 5, 6 or 8: CTAs per SM the group walk's register
  *       budget is set for), "bh.acc_smem" (1: the 64-body walk keeps its
  *       accumulators in shared memory, the default; 0: in registers),
  *       "bh.eval_unroll" (1, 2 or 4: unroll of the interaction-list loop of
- *       the 64-body, register-accumulator, 4-CTA build). */
+ *       the 64-body walk, at 5 CTAs per SM with shared-memory accumulators
+ *       or at 4 with register accumulators)). */
 nbg_status nbg_tune_set(nbg_engine* e, const char* key, int64_t value);
 nbg_status nbg_tune_get(nbg_engine* e, const char* key, int64_t* value);
 
