@@ -261,7 +261,8 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       "bh.order" (1: monopole cells as the reference; 2: accepted cells
  *       add their quadrupole term, from FP32 second moments per node),
  *       "bh.walk_blocks" (4, 5, 6 or 8: CTAs per SM the group walk's register
- *       budget is set for), "bh.acc_smem" (1: the 64-body walk keeps its
+ *       budget is set for; the quadrupole walk of 64-body groups takes 3,
+ *       its default, or 4), "bh.acc_smem" (1: the 64-body walk keeps its
  *       accumulators in shared memory, the default; 0: in registers),
  *       "bh.eval_unroll" (1, 2 or 4: unroll of the interaction-list loop of
  *       the 64-body walk, at 5 CTAs per SM with shared-memory accumulators

@@ -868,8 +868,8 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
     const bool clamp = !(e->params.softening > 0.0);
     if (e->tune_get("bh.walk", 1) == 1 && n >= 32) {
         // "bh.group": bodies per warp group (32 or 64); "bh.walk_blocks":
-        // CTAs per SM the kernel's register budget is set for (4, 5, 6 or 8:
-        // 128, 102, 80 or 64 registers)
+        // CTAs per SM the kernel's register budget is set for (3, 4, 5, 6 or
+        // 8: 168, 128, 102, 80 or 64 registers; 3 for quadrupole cells only)
         // "bh.order": 1 monopole cells, 2 monopole + quadrupole cells
         const int order = e->tune_get("bh.order", 1) >= 2 ? 2 : 1;
         if (order == 2) {
@@ -883,12 +883,17 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
         // 64-body groups keep their accumulators in shared memory by default
         // and run 5 CTAs per SM ("bh.acc_smem" = 0: registers, 4 CTAs)
         const bool acc_smem = bpl == 2 && order == 1 && e->tune_get("bh.acc_smem", 1) != 0;
-        const int64_t wb = e->tune_get("bh.walk_blocks", bpl == 2 ? (acc_smem ? 5 : 4) : 6);
+        // the quadrupole walk of 64-body groups runs 3 CTAs per SM by default
+        // (164 registers, no spill; at 4 CTAs it spills and is 5 % slower)
+        const int64_t wb = e->tune_get("bh.walk_blocks",
+                                       bpl == 2 ? (order == 2 ? 3 : acc_smem ? 5 : 4) : 6);
         using WalkKernel = void (*)(const double*, double*, int, float, TreeState, int, unsigned*);
         WalkKernel kern;
 #define NBG_GW(C, B) (wb >= 8 ? bh_group_walk_kernel<C, 8, B, 1> : wb >= 6 ? bh_group_walk_kernel<C, 6, B, 1> \
                       : wb >= 5 ? bh_group_walk_kernel<C, 5, B, 1> : bh_group_walk_kernel<C, 4, B, 1>)
-        if (order == 2)  // one register budget per group size
+        if (order == 2 && bpl == 2 && wb <= 3)
+            kern = clamp ? bh_group_walk_kernel<true, 3, 2, 2> : bh_group_walk_kernel<false, 3, 2, 2>;
+        else if (order == 2)
             kern = bpl == 2 ? (clamp ? bh_group_walk_kernel<true, 4, 2, 2> : bh_group_walk_kernel<false, 4, 2, 2>)
                             : (clamp ? bh_group_walk_kernel<true, 5, 1, 2> : bh_group_walk_kernel<false, 5, 1, 2>);
         else if (acc_smem) {

@@ -83,6 +83,11 @@ extern "C" nbg_status nbg_autotune(nbg_engine* e, int reps, char* report, size_t
     std::vector<Candidate> cands;
     if (e->params.precision == NBG_PREC_FP64 || (e->params.algo == NBG_ALGO_BH && e->params.learned)) {
         cands.push_back({});  // one fixed kernel: nothing to choose
+    } else if (e->params.algo == NBG_ALGO_BH && e->tune_get("bh.order", 1) >= 2) {
+        // quadrupole cells: the group walks that add the term (the coherent
+        // walk does not, so it is no candidate)
+        for (int b : {3, 4}) cands.push_back({{"bh.walk", 1}, {"bh.group", 64}, {"bh.walk_blocks", b}});
+        cands.push_back({{"bh.walk", 1}, {"bh.group", 32}});
     } else if (e->params.algo == NBG_ALGO_BH) {
         for (int b : {5, 4})
             cands.push_back({{"bh.walk", 1}, {"bh.group", 64}, {"bh.walk_blocks", b}, {"bh.acc_smem", 1}});

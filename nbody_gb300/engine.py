@@ -542,8 +542,10 @@ class NbodyEngineGB300:
         p = self._params
         algo = "bh" if p.algo == 1 else "direct"
         prec = "fp64" if p.precision == 0 else "mixed"
+        order = self.tune_get("bh.order") if algo == "bh" else None
         return f"{algo}/{prec}/{'soft' if p.softening > 0 else 'clamp'}" + \
-            ("/learned" if p.learned else "")
+            ("/learned" if p.learned else "") + \
+            ("/quadrupole" if order is not None and order >= 2 else "")
 
     @property
     def device(self) -> int:

@@ -116,6 +116,35 @@ def test_engine_autotune_bh(make_engine):
 
 
 @pytest.mark.gpu
+def test_engine_autotune_bh_quadrupole(make_engine):
+    """With quadrupole cells only the group walks, which add the term, are
+    candidates; every candidate gives forces of the same accuracy."""
+    d = NBodyData.plummer(1 << 14, seed=22)
+    e = make_engine(algo="bh", precision="mixed", softening=1e-3, distance_to_node_radius_ratio=2.0)
+    e.tune_set("bh.order", 2)
+    assert e.init(d)
+    y = e.get_y()
+    f = e.create_buffer(8 * 6 * (1 << 14))
+    e.fcompute(0.0, y, f)
+    f0 = np.zeros(6 * (1 << 14))
+    e.read_buffer(f0, f)
+    rep = e.autotune(2)
+    keys = [c["keys"] for c in rep["candidates"]]
+    assert keys == [{"bh.walk": 1, "bh.group": 64, "bh.walk_blocks": b} for b in (3, 4)] + \
+        [{"bh.walk": 1, "bh.group": 32}]
+    e.fcompute(0.0, y, f)
+    f1 = np.zeros(6 * (1 << 14))
+    e.read_buffer(f1, f)
+    if rep["best"]["bh.group"] == 64:  # same walk, another register budget: the same sums
+        assert np.array_equal(f0, f1)
+    else:
+        n = 1 << 14
+        a0, a1 = f0[3 * n:].reshape(3, n).T, f1[3 * n:].reshape(3, n).T
+        rel = np.linalg.norm(a1 - a0, axis=1) / np.linalg.norm(a0, axis=1)
+        assert np.median(rel) < 1e-2
+
+
+@pytest.mark.gpu
 def test_ensemble_autotune_keeps_results():
     from nbody_gb300.ensemble import Ensemble
     rng = np.random.default_rng(3)
