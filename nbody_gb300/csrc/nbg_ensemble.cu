@@ -646,15 +646,14 @@ nbg_status nbg_ensemble_fcompute(nbg_ensemble* s, double* f) {
 nbg_status nbg_ensemble_statistics(nbg_ensemble* s, double* out) {
     if (s == nullptr || out == nullptr) return NBG_ERR_INVALID_ARG;
     nbg_engine* e = s->eng;
-    double* d_out = nullptr;
-    NBG_CUDA(e, cudaMalloc(&d_out, 12 * (size_t)s->nsys * sizeof(double)));
+    DevScratch res;
+    NBG_CUDA(e, cudaMalloc(&res.p, 12 * (size_t)s->nsys * sizeof(double)));
     nbg_status st = stats_segments(e, s->y, s->mass, s->B, s->nsys, s->off, s->cnt,
                                    s->h_off.data(), s->h_cnt.data(),
-                                   s->p.softening * s->p.softening, d_out);
+                                   s->p.softening * s->p.softening, res.as<double>());
     if (st == NBG_OK)
-        NBG_CUDA(e, cudaMemcpy(out, d_out, 12 * (size_t)s->nsys * sizeof(double),
+        NBG_CUDA(e, cudaMemcpy(out, res.p, 12 * (size_t)s->nsys * sizeof(double),
                                cudaMemcpyDeviceToHost));
-    cudaFree(d_out);
     return st;
 }
 

@@ -172,8 +172,9 @@ nbg_status stats_segments(nbg_engine* e, const double* y, const double* mass, si
     for (int s = 0; s < nsys; ++s)
         for (int i0 = 0; i0 < h_cnt[s]; i0 += kStatThreads) units.push_back(PairUnit{s, i0});
     (void)h_off;
-    PairUnit* d_units = nullptr;
-    NBG_CUDA(e, cudaMalloc(&d_units, units.size() * sizeof(PairUnit) + 16));
+    DevScratch units_buf;
+    NBG_CUDA(e, cudaMalloc(&units_buf.p, units.size() * sizeof(PairUnit) + 16));
+    PairUnit* d_units = units_buf.as<PairUnit>();
     NBG_CUDA(e, cudaMemcpyAsync(d_units, units.data(), units.size() * sizeof(PairUnit),
                                 cudaMemcpyHostToDevice, e->stream));
     NBG_CUDA(e, cudaMemsetAsync(d_out, 0, 12 * (size_t)nsys * sizeof(double), e->stream));
@@ -185,8 +186,7 @@ nbg_status stats_segments(nbg_engine* e, const double* y, const double* mass, si
                                                                      d_units, eps2, d_out);
         NBG_LAUNCHED(e, "stats_potential_kernel");
     }
-    NBG_CUDA(e, cudaStreamSynchronize(e->stream));
-    cudaFree(d_units);
+    NBG_CUDA(e, cudaStreamSynchronize(e->stream));  // before units_buf is freed
     return NBG_OK;
 }
 
@@ -202,22 +202,17 @@ extern "C" nbg_status nbg_statistics(nbg_engine* e, const nbg_buffer* y, double 
         return set_error(e, NBG_ERR_SIZE_MISMATCH, "y smaller than 6N doubles");
     long long h_off = 0;
     int h_cnt = (int)e->count;
-    long long* d_off = nullptr;
-    int* d_cnt = nullptr;
-    double* d_out = nullptr;
-    NBG_CUDA(e, cudaMalloc(&d_off, sizeof(long long)));
-    NBG_CUDA(e, cudaMalloc(&d_cnt, sizeof(int)));
-    NBG_CUDA(e, cudaMalloc(&d_out, 12 * sizeof(double)));
-    NBG_CUDA(e, cudaMemcpyAsync(d_off, &h_off, sizeof(h_off), cudaMemcpyHostToDevice, e->stream));
-    NBG_CUDA(e, cudaMemcpyAsync(d_cnt, &h_cnt, sizeof(h_cnt), cudaMemcpyHostToDevice, e->stream));
+    DevScratch off, cnt, res;
+    NBG_CUDA(e, cudaMalloc(&off.p, sizeof(long long)));
+    NBG_CUDA(e, cudaMalloc(&cnt.p, sizeof(int)));
+    NBG_CUDA(e, cudaMalloc(&res.p, 12 * sizeof(double)));
+    NBG_CUDA(e, cudaMemcpyAsync(off.p, &h_off, sizeof(h_off), cudaMemcpyHostToDevice, e->stream));
+    NBG_CUDA(e, cudaMemcpyAsync(cnt.p, &h_cnt, sizeof(h_cnt), cudaMemcpyHostToDevice, e->stream));
     nbg_status s = stats_segments(e, static_cast<const double*>(y->dptr), e->d_mass, e->count, 1,
-                                  d_off, d_cnt, &h_off, &h_cnt,
-                                  e->params.softening * e->params.softening, d_out);
+                                  off.as<long long>(), cnt.as<int>(), &h_off, &h_cnt,
+                                  e->params.softening * e->params.softening, res.as<double>());
     if (s == NBG_OK) {
-        NBG_CUDA(e, cudaMemcpy(out, d_out, 12 * sizeof(double), cudaMemcpyDeviceToHost));
+        NBG_CUDA(e, cudaMemcpy(out, res.p, 12 * sizeof(double), cudaMemcpyDeviceToHost));
     }
-    cudaFree(d_off);
-    cudaFree(d_cnt);
-    cudaFree(d_out);
     return s;
 }

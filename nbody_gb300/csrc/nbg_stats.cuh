@@ -7,6 +7,20 @@
 
 namespace nbg {
 
+// A device allocation freed when it leaves scope: the statistics calls
+// allocate small per-call arrays, and an early error return must not leak them.
+struct DevScratch {
+    void* p = nullptr;
+    DevScratch() = default;
+    DevScratch(const DevScratch&) = delete;
+    DevScratch& operator=(const DevScratch&) = delete;
+    ~DevScratch() {
+        if (p != nullptr) cudaFree(p);
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
 // Systems s = 0..nsys-1 occupy bodies [off[s], off[s] + cnt[s]) of SoA state
 // y with the given stride.  d_out receives 12 doubles per system; eps2 is
 // the softening of the pair potential (0 = the reference's potential).
