@@ -85,17 +85,20 @@ struct PairUnit {
     int i0;  // first body (system-local) of the 256-body block
 };
 
-// 1 / sqrt(x) in FP64: the FP32 hardware estimate (about 23 correct bits)
-// refined by two Newton-Raphson steps y <- y (3 - x y^2) / 2 (each doubles
-// the correct bits), so the result is within a few ulp of the correctly
-// rounded value; outside the FP32 range the division form is used.
+// 1 / sqrt(x) in FP64: the FP32 hardware estimate y0 (about 23 correct
+// bits) refined by one second-order step of the series
+// (1 - e)^(-1/2) = 1 + e/2 + 3e^2/8 + ..., e = 1 - x y0^2 (Householder's
+// iteration of order 2), which leaves a truncation error of order e^3,
+// below 2^-60 relative: the result is within a few ulp of the correctly
+// rounded value, for 5 FP64 operations.  Inputs whose FP32 image is not a
+// positive normal number (zero, subnormal, infinite, NaN, negative) take
+// the division form; the test is integer arithmetic on the FP32 bits.
 __device__ __forceinline__ double rsqrt_fp64(double x) {
-    if (!(x > 1e-30 && x < 1e30)) return 1.0 / sqrt(x);
-    double y = (double)rsqrtf((float)x);
-    const double h = 0.5 * x;
-    y = y * fma(-h * y, y, 1.5);
-    y = y * fma(-h * y, y, 1.5);
-    return y;
+    const float xf = (float)x;
+    if (__float_as_uint(xf) - 0x00800000u >= 0x7f000000u) return 1.0 / sqrt(x);
+    const double y0 = (double)rsqrtf(xf);
+    const double e = fma(-x * y0, y0, 1.0);
+    return fma(y0 * e, fma(e, 0.375, 0.5), y0);
 }
 
 // Potential energy: one CTA per (system, 256 i-bodies); FP64 pair sums over
@@ -142,19 +145,19 @@ stats_potential_kernel(const double* __restrict__ y, const double* __restrict__ 
         double tile = 0.0;
         // the own tile skips the self pair; without softening, pairs closer
         // than kMinDistance add nothing
-        auto term = [&](int k) {
+        auto add = [&](int k) {
             const double dx = xi - tx[k], dy = yi - ty[k], dz = zi - tz[k];
             const double r2 = dx * dx + dy * dy + dz * dz;
-            if (!SOFT && r2 < kMinDistance) return 0.0;
-            return tm[k] * rsqrt_fp64(r2 + eps2);
+            if (!SOFT && r2 < kMinDistance) return;
+            tile = fma(-tm[k], rsqrt_fp64(SOFT ? r2 + eps2 : r2), tile);
         };
         if (own) {
             for (int k = 0; k < c; ++k)
-                if (j0 + k != li) tile -= term(k);
+                if (j0 + k != li) add(k);
             pe += tile;
         } else {
 #pragma unroll 4
-            for (int k = 0; k < c; ++k) tile -= term(k);
+            for (int k = 0; k < c; ++k) add(k);
             pe += 2.0 * tile;
         }
     }
