@@ -264,6 +264,9 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       budget is set for; the quadrupole walk of 64-body groups takes 3,
  *       its default, or 4), "bh.acc_smem" (1: the 64-body walk keeps its
  *       accumulators in shared memory, the default; 0: in registers),
+ *       "bh.persistent" (1, the default: the group walk runs as many CTAs
+ *       as fit at once, its warps taking groups from a counter; 0: one CTA
+ *       per four groups),
  *       "bh.eval_unroll" (1, 2 or 4: unroll of the interaction-list loop of
  *       the 64-body walk, at 5 CTAs per SM with shared-memory accumulators
  *       or at 4 with register accumulators)). */

@@ -24,6 +24,17 @@ def test_header_lists_match(gpulib):
     assert set(_lib.EXPORTS) <= set(declared), set(_lib.EXPORTS) - set(declared)
 
 
+def test_tuning_keys_documented():
+    """Every tuning key the library reads is documented in the header."""
+    used = set()
+    for src in (ROOT / "nbody_gb300" / "csrc").glob("*.cu"):
+        used |= set(re.findall(r'tune_get\("([a-z0-9_.]+)"', src.read_text()))
+    assert {"bh.walk", "direct.symmetric", "ensemble.unroll"} <= used
+    header = (ROOT / "include" / "nbody_gb300.h").read_text()
+    missing = sorted(k for k in used if f'"{k}"' not in header)
+    assert not missing, f"tuning keys read but not documented: {missing}"
+
+
 def test_status_strings_and_version(gpulib):
     assert gpulib.nbg_abi_version() == 1
     assert gpulib.nbg_status_string(0) == b"ok"
