@@ -204,7 +204,8 @@ constexpr int kCapSamples = 32;
 
 // Second list of the quadrupole walk (bh.order = 2): accepted cells with their
 // second moments; leaves stay in the monopole list.  Arrays in the order
-// x, y, z, m, Mxx, Myy, Mzz, tr M / 2, Mxy, Mxz, Myz.
+// x, y, z, m, Sxx, Syy, Szz, tr S / 2, Sxy, Sxz, Syz, S = -3 M (the moments
+// as stored, scaled so that the walk's term needs no constant factor).
 constexpr int kGWQList = 128;
 constexpr int kGWQFields = 11;
 struct QuadLists {
@@ -215,7 +216,9 @@ struct QuadLists {
 // central moments M) on a body at x, for two cells at once; d = c - x:
 //   a = d (m / r^3 - 3 k / r^5) - (3 / r^5) M d,  k = tr M / 2 - (5/2) (d.M.d) / r^2,
 // from the expansion of 1 / |r - s| about the mass centre to second order
-// (the first-order term vanishes there).
+// (the first-order term vanishes there).  With the stored S = -3 M:
+//   a = d (m / r^3 + k' / r^5) + (S d) / r^5,  k' = tr S / 2 - (5/2) (d.S.d) / r^2
+// (31 packed operations for two cells).
 template <bool CLAMP>
 __device__ __forceinline__ void quad_pair(const f2_t* q, f2_t xi, f2_t yi, f2_t zi, f2_t eps2,
                                           f2_t& ax, f2_t& ay, f2_t& az) {
@@ -234,17 +237,17 @@ __device__ __forceinline__ void quad_pair(const f2_t* q, f2_t xi, f2_t yi, f2_t 
     const f2_t inv = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
     const f2_t inv2 = f2_mul(inv, inv);
     const f2_t inv3 = f2_mul(inv2, inv);
-    const f2_t c3 = f2_mul(f2_mul(inv3, inv2), f2_pack(-3.f, -3.f));  // -3 / r^5
-    // M d with M = [[xx, xy, xz], [xy, yy, yz], [xz, yz, zz]]
-    const f2_t mdx = f2_fma(q[9], dz, f2_fma(q[8], dy, f2_mul(q[4], dx)));
-    const f2_t mdy = f2_fma(q[10], dz, f2_fma(q[5], dy, f2_mul(q[8], dx)));
-    const f2_t mdz = f2_fma(q[6], dz, f2_fma(q[10], dy, f2_mul(q[9], dx)));
-    const f2_t dmd = f2_fma(dz, mdz, f2_fma(dy, mdy, f2_mul(dx, mdx)));
-    const f2_t k = f2_fma(f2_mul(dmd, inv2), f2_pack(-2.5f, -2.5f), q[7]);
-    const f2_t cd = f2_fma(c3, k, f2_mul(q[3], inv3));
-    ax = f2_fma(c3, mdx, f2_fma(cd, dx, ax));
-    ay = f2_fma(c3, mdy, f2_fma(cd, dy, ay));
-    az = f2_fma(c3, mdz, f2_fma(cd, dz, az));
+    const f2_t inv5 = f2_mul(inv3, inv2);
+    // S d with S = [[xx, xy, xz], [xy, yy, yz], [xz, yz, zz]]
+    const f2_t sdx = f2_fma(q[9], dz, f2_fma(q[8], dy, f2_mul(q[4], dx)));
+    const f2_t sdy = f2_fma(q[10], dz, f2_fma(q[5], dy, f2_mul(q[8], dx)));
+    const f2_t sdz = f2_fma(q[6], dz, f2_fma(q[10], dy, f2_mul(q[9], dx)));
+    const f2_t dsd = f2_fma(dz, sdz, f2_fma(dy, sdy, f2_mul(dx, sdx)));
+    const f2_t k = f2_fma(f2_mul(dsd, inv2), f2_pack(-2.5f, -2.5f), q[7]);
+    const f2_t cd = f2_fma(inv5, k, f2_mul(q[3], inv3));
+    ax = f2_fma(inv5, sdx, f2_fma(cd, dx, ax));
+    ay = f2_fma(inv5, sdy, f2_fma(cd, dy, ay));
+    az = f2_fma(inv5, sdz, f2_fma(cd, dz, az));
 }
 
 template <bool CLAMP>
@@ -736,17 +739,18 @@ bh_body_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n,
                 const float s3 = __ldg(&t.nodem[c]) * inv3;
                 float ax = dx * s3, ay = dy * s3, az = dz * s3;
                 if (ORDER == 2 && c < n) {
-                    // a += d (-3 k / r^5) - (3 / r^5) M d, k = tr M / 2 - 2.5 dMd / r^2
+                    // a += d k' / r^5 + (S d) / r^5, k' = tr S / 2 - 2.5 dSd / r^2,
+                    // with the stored S = -3 M
                     const float4 q0 = __ldg(&t.quad[2 * c]), q1 = __ldg(&t.quad[2 * c + 1]);
-                    const float c3 = -3.f * inv3 * inv2;
-                    const float mx = fmaf(q1.y, dz, fmaf(q1.x, dy, q0.x * dx));
-                    const float my = fmaf(q1.z, dz, fmaf(q0.y, dy, q1.x * dx));
-                    const float mz = fmaf(q0.z, dz, fmaf(q1.z, dy, q1.y * dx));
-                    const float dmd = fmaf(dz, mz, fmaf(dy, my, dx * mx));
-                    const float ck = c3 * fmaf(-2.5f * dmd, inv2, q0.w);
-                    ax += fmaf(ck, dx, c3 * mx);
-                    ay += fmaf(ck, dy, c3 * my);
-                    az += fmaf(ck, dz, c3 * mz);
+                    const float inv5 = inv3 * inv2;
+                    const float sx = fmaf(q1.y, dz, fmaf(q1.x, dy, q0.x * dx));
+                    const float sy = fmaf(q1.z, dz, fmaf(q0.y, dy, q1.x * dx));
+                    const float sz = fmaf(q0.z, dz, fmaf(q1.z, dy, q1.y * dx));
+                    const float dsd = fmaf(dz, sz, fmaf(dy, sy, dx * sx));
+                    const float ck = inv5 * fmaf(-2.5f * dsd, inv2, q0.w);
+                    ax += fmaf(ck, dx, inv5 * sx);
+                    ay += fmaf(ck, dy, inv5 * sy);
+                    az += fmaf(ck, dz, inv5 * sz);
                 }
                 add(hx, lx, ax);
                 add(hy, ly, ay);
@@ -802,13 +806,16 @@ __device__ __forceinline__ void quad_node(size_t idx, TreeState& t) {
         const float4 cc = t.node4[c];
         const float mc = t.nodem[c];
         const float4 q0 = t.quad[2 * c], q1 = t.quad[2 * c + 1];
+        // parallel-axis shift of the child's moments, in the stored scale
+        // S = -3 M
         const float dx = cc.x - pc.x, dy = cc.y - pc.y, dz = cc.z - pc.z;
-        xx += q0.x + mc * dx * dx;
-        yy += q0.y + mc * dy * dy;
-        zz += q0.z + mc * dz * dz;
-        xy += q1.x + mc * dx * dy;
-        xz += q1.y + mc * dx * dz;
-        yz += q1.z + mc * dy * dz;
+        const float w = -3.f * mc;
+        xx += q0.x + w * dx * dx;
+        yy += q0.y + w * dy * dy;
+        zz += q0.z + w * dz * dz;
+        xy += q1.x + w * dx * dy;
+        xz += q1.y + w * dx * dz;
+        yz += q1.z + w * dy * dz;
     }
     t.quad[2 * idx] = make_float4(xx, yy, zz, 0.5f * (xx + yy + zz));
     t.quad[2 * idx + 1] = make_float4(xy, xz, yz, 0.f);

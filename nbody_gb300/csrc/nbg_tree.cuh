@@ -49,8 +49,9 @@ struct TreeState {
     // learned-correction node features (quadrupole, spread), see nbg_learned.cu
     float4* feat = nullptr;   // [3][size] or null
 
-    // quadrupole walk records (nbg_bh.cu): second central mass moments,
-    // quad[2 idx] = (Mxx, Myy, Mzz, tr M / 2), quad[2 idx + 1] = (Mxy, Mxz, Myz, 0)
+    // quadrupole walk records (nbg_bh.cu): second central mass moments M
+    // stored as S = -3 M, quad[2 idx] = (Sxx, Syy, Szz, tr S / 2),
+    // quad[2 idx + 1] = (Sxy, Sxz, Syz, 0)
     float4* quad = nullptr;   // [2][size] or null
 
     // walk counters: node tests, interactions, deepest group-walk stack,
