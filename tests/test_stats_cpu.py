@@ -3,7 +3,8 @@
 y = y0 + y0 e (1/2 + 3e/8) with e = 1 - x y0^2, the second-order step of the
 series (1 - e)^(-1/2) = 1 + e/2 + 3e^2/8 + ...  The GPU kernel's sums are
 checked against the oracle by tests/test_stats_gpu.py; this pins the step's
-accuracy for estimates as far off as the hardware's."""
+accuracy for estimates as far off as the hardware's, and the kernel's tile
+schedule (each unordered pair once) for every block count."""
 import numpy as np
 import pytest
 
@@ -37,3 +38,26 @@ def test_one_newton_step_would_not_be():
     exact = 1.0 / np.sqrt(x.astype(np.longdouble))
     rel = np.abs((newton.astype(np.longdouble) - exact) / exact).astype(np.float64)
     assert rel.min() > 1e3 * 2.0 ** -53
+
+
+@pytest.mark.parametrize("nb", list(range(1, 18)) + [32, 33, 512])
+def test_cyclic_tile_schedule_counts_each_pair_once(nb):
+    """The potential kernel's schedule (stats_potential_kernel): block b takes
+    tiles (b + t) mod nb for t = 0 .. last, last = nb/2 - 1 for the upper half
+    of an even nb and nb/2 otherwise; its own tile counts both orders of each
+    pair (weight 1), the others one order (weight 2).  Every unordered tile
+    pair must then carry weight 2 in total, and the blocks' loads differ by at
+    most one tile."""
+    weight = np.zeros((nb, nb))
+    loads = []
+    for b in range(nb):
+        last = nb // 2 - 1 if (nb % 2 == 0 and b >= nb // 2) else nb // 2
+        loads.append(last + 1)
+        for t in range(last + 1):
+            j = (b + t) % nb
+            if t == 0:
+                weight[b, b] += 2  # both orders of each pair inside the tile
+            else:
+                weight[min(b, j), max(b, j)] += 2
+    assert np.all(weight[np.triu_indices(nb)] == 2)
+    assert max(loads) - min(loads) <= 1
