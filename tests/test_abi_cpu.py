@@ -24,6 +24,20 @@ def test_header_lists_match(gpulib):
     assert set(_lib.EXPORTS) <= set(declared), set(_lib.EXPORTS) - set(declared)
 
 
+@pytest.mark.parametrize("lang,std", [("c", "-std=c99"), ("c++", "-std=c++17")])
+def test_header_compiles_standalone(lang, std):
+    """The C ABI header is self-contained C and C++ (the reference-side adapter
+    includes it from C++; a C or FFI host may include it from C)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    r = subprocess.run([cc, std, "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-x", lang,
+                        str(ROOT / "include" / "nbody_gb300.h")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_tuning_keys_documented():
     """Every tuning key the library reads is documented in the header."""
     used = set()
