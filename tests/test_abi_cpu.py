@@ -38,6 +38,25 @@ def test_header_compiles_standalone(lang, std):
     assert r.returncode == 0, r.stderr
 
 
+def test_ctypes_prototypes_match_header():
+    """Every ctypes prototype in nbody_gb300/_lib.py takes as many arguments
+    as the header declares for that function."""
+    import ast
+    text = (ROOT / "include" / "nbody_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    declared = {}
+    for m in re.finditer(r"\b(nbg_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+        params = m.group(2).strip()
+        declared[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    tree = ast.parse((ROOT / "nbody_gb300" / "_lib.py").read_text())
+    proto = {node.args[1].value: len(node.args) - 3 for node in ast.walk(tree)
+             if isinstance(node, ast.Call) and getattr(node.func, "id", None) == "_proto"}
+    assert set(proto) == set(declared), set(proto) ^ set(declared)
+    wrong = {k: (declared[k], v) for k, v in proto.items() if declared[k] != v}
+    assert not wrong, f"argument counts (header, ctypes) differ: {wrong}"
+
+
 def test_tuning_keys_documented():
     """Every tuning key the library reads is documented in the header."""
     used = set()
