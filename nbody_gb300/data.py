@@ -251,8 +251,7 @@ class NBodyData:
         center = np.array([sx * 0.5, sy * 0.5, sz * 0.5])
         base = np.array([radius, 0.0, 0.0])
         f = _force(np.zeros(3), base, galaxy_mass, galaxy_mass)
-        vel = np.array([0.0, math.sqrt(np.linalg.norm(f) * np.linalg.norm(base)
-                                       / (2 * galaxy_mass)), 0.0])
+        vel = np.array([0.0, math.sqrt(_length(f) * _length(base) / (2 * galaxy_mass)), 0.0])
         parts = [_galaxy(center - base, vel / 3, radius, galaxy_mass, star_count),
                  _galaxy(center + base, -vel / 3, radius, galaxy_mass, star_count)]
         d.vertices = np.concatenate([p[0] for p in parts])
@@ -330,10 +329,26 @@ def _iso(rng, n):
     return np.stack([s * np.cos(phi), s * np.sin(phi), z], axis=1)
 
 
+def _norm2(v) -> float:
+    """x x + y y + z z in the reference's order (nbody/vertex.h:151-158)."""
+    x, y, z = float(v[0]), float(v[1]), float(v[2])
+    return x * x + y * y + z * z
+
+
+def _length(v) -> float:
+    return math.sqrt(_norm2(v))
+
+
+def _cross(a, b):
+    """nbody/vertex.h:133-138."""
+    return np.array([a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2],
+                     a[0] * b[1] - a[1] * b[0]])
+
+
 def _force(v1, v2, m1, m2):
     """nbody/nbody_data.cpp:35-44."""
     dr = v1 - v2
-    r2 = float(dr @ dr)
+    r2 = _norm2(dr)
     r2 = max(r2, MIN_DISTANCE)
     return dr * ((-m1 * m2) / (r2 * math.sqrt(r2)))
 
@@ -398,19 +413,24 @@ def _galaxy(center, velocity, radius, total_mass, count):
     mass = [bh_mass]
     n = 0
     while n != count:
-        r = np.array([uniform(), uniform(), uniform()])
-        rlen = float(np.linalg.norm(r))
+        # nbvertex_t r(uniform(rng), uniform(rng), uniform(rng)): C++ leaves the
+        # order of the three draws unspecified; g++ evaluates the constructor's
+        # arguments last to first, so the first draw is z and the last is x
+        # (checked against the reference's own build)
+        u1, u2, u3 = uniform(), uniform(), uniform()
+        r = np.array([u3, u2, u1])
+        rlen = _length(r)
         if rlen > radius:
             continue
         r[2] *= 0.3
         r = r + center
-        v = np.cross(r - center, up)
-        if np.linalg.norm(v) < 1e-7:
-            v = np.cross(r - center, right)
-        v = v / np.linalg.norm(v)
+        v = _cross(r - center, up)
+        if _length(v) < 1e-7:
+            v = _cross(r - center, right)
+        v = v / _length(v)
         eff = (rlen / radius) ** 3.0 * all_stars + bh_mass
         fr = _force(r, center, star_mass, eff)
-        v = v * math.sqrt(np.linalg.norm(fr) * np.linalg.norm(r - center) / star_mass)
+        v = v * math.sqrt(_length(fr) * _length(r - center) / star_mass)
         pos.append(r)
         vel.append(v + velocity)
         mass.append(star_mass)

@@ -16,7 +16,9 @@ solver classes drive any engine:
                    rkf  (nbody/nbody_solver_rkf.cpp:30-71),
                    rkdverk (nbody/nbody_solver_rkdverk.cpp:29-70),
                    rkgl (nbody/nbody_solver_rkgl.cpp:29-60, implicit),
-                   rklc (nbody/nbody_solver_rklc.cpp:29-60, implicit)
+                   rklc (nbody/nbody_solver_rklc.cpp:29-60, implicit),
+                   rkfeagin10/12/14 (nbody/nbody_solver_rkfeagin{10,12,14}.cpp,
+                   loaded from feagin_tables.json)
   * midpoint       nbody/nbody_solver_midpoint.cpp:23-40
   * midpoint-st    nbody/nbody_solver_midpoint_stetter.cpp:23-76
   * trapeze        nbody/nbody_solver_trapeze.cpp:30-56
@@ -30,7 +32,8 @@ The Butcher coefficients are the published Dormand-Prince, Cash-Karp,
 Fehlberg, Verner (DVERK 6(5)), Gauss-Legendre and Lobatto IIIC tables,
 written out in the same row layout the reference uses (the Gauss-Legendre
 entries with the same double expressions in sqrt(15)).  The Feagin 10/12/14
-tables are not restated.
+tables (hundreds of 60-digit published coefficients) are data: the doubles
+the reference's solvers hold, in feagin_tables.json.
 """
 from __future__ import annotations
 
@@ -125,8 +128,26 @@ RKLC = ButcherTable(
     [Fr(1, 6), Fr(2, 3), Fr(1, 6)], [Fr(-1, 2), 2, Fr(-1, 2)], [0, Fr(1, 2), 1],
     embedded=True, implicit=True)
 
+def _feagin_tables() -> dict:
+    """The Feagin 10(8), 12(10) and 14(12) tables (nbody/nbody_solver_rkfeagin
+    {10,12,14}.cpp: 17, 25 and 35 stages of T. Feagin's published 60-digit
+    coefficients, as doubles), from feagin_tables.json beside this module
+    (each double stored exactly, as float.hex)."""
+    import json
+    from pathlib import Path
+    data = json.loads((Path(__file__).resolve().parent / "feagin_tables.json").read_text())
+    out = {}
+    for name, t in data["tables"].items():
+        h = float.fromhex
+        out[name] = ButcherTable([[h(x) for x in row] for row in t["a"]],
+                                 [h(x) for x in t["b1"]], [h(x) for x in t["b2"]],
+                                 [h(x) for x in t["c"]], embedded=t["embedded"],
+                                 implicit=t["implicit"])
+    return out
+
+
 TABLES = {"rkdp": RKDP, "rkck": RKCK, "rkf": RKF, "rkdverk": RKDVERK, "rkgl": RKGL,
-          "rklc": RKLC}
+          "rklc": RKLC, **_feagin_tables()}
 
 
 class Solver:
@@ -247,6 +268,12 @@ class SolverRKButcher(Solver):
         self._ycorr = None
         self._tcorr = None
         self.last_error = 0.0
+        # instrumentation (no effect on the integration): accepted substeps,
+        # those accepted above the threshold (at the recursion cap or the
+        # minimum step), and the largest error of an accepted substep
+        self.accepted_steps = 0
+        self.capped_steps = 0
+        self.max_accepted_error = 0.0
 
     def advise(self, dt: float) -> None:
         e = self._engine
@@ -325,6 +352,9 @@ class SolverRKButcher(Solver):
                 self._sub_step(self.substep_subdivisions, t, new_dt, cy, level + 1)
                 e.copy_buffer(y, cy)
             else:
+                self.accepted_steps += 1
+                self.capped_steps += int(max_error > self.error_threshold)
+                self.max_accepted_error = max(self.max_accepted_error, max_error)
                 coeff = [bt.b2[n] * dt for n in range(bt.steps)]
                 if self.correction:
                     e.fmaddn_corr(y, self._ycorr, self._k, coeff, len(self._k))

@@ -41,6 +41,15 @@ def build_oracle(force: bool = False) -> Path:
     return LIB
 
 
+class _Heap(C.Structure):
+    """struct orc_heap (nbody_oracle.h)."""
+    _fields_ = [("count", C.c_size_t), ("size", C.c_size_t),
+                ("com", C.POINTER(C.c_double)), ("mass", C.POINTER(C.c_double)),
+                ("r2", C.POINTER(C.c_double)), ("bmin", C.POINTER(C.c_double)),
+                ("bmax", C.POINTER(C.c_double)), ("body_n", C.POINTER(C.c_int64)),
+                ("lambda2", C.c_double)]
+
+
 class Oracle:
     """Thin numpy-facing wrapper over the oracle C functions."""
 
@@ -145,6 +154,30 @@ class Oracle:
                 out.append(f)
                 if mutate is not None:
                     y = np.ascontiguousarray(mutate(y))
+        finally:
+            self.lib.orc_heap_free(C.addressof(heap))
+        return out
+
+    def heap_nodes(self, y, mass, lam):
+        """The kd heap's node arrays after orc_heap_build: (com [3][2n],
+        mass [2n], crit r^2 [2n], body [2n], bmin [3][2n], bmax [3][2n])."""
+        heap = _Heap()
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        mass = np.ascontiguousarray(mass, dtype=np.float64)
+        n = mass.size
+        try:
+            rc = self.lib.orc_heap_build(C.addressof(heap), n, y[:n].copy(), y[n:2 * n].copy(),
+                                         y[2 * n:3 * n].copy(), mass, lam)
+            if rc != 0:
+                raise ValueError("heap build failed")
+            sz = heap.size
+
+            def arr(p, k):
+                return np.ctypeslib.as_array(p, shape=(k,)).copy()
+            com = arr(heap.com, 3 * sz).reshape(sz, 3).T.copy()
+            out = (com, arr(heap.mass, sz), arr(heap.r2, sz), arr(heap.body_n, sz),
+                   arr(heap.bmin, 3 * sz).reshape(sz, 3).T.copy(),
+                   arr(heap.bmax, 3 * sz).reshape(sz, 3).T.copy())
         finally:
             self.lib.orc_heap_free(C.addressof(heap))
         return out

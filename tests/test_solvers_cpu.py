@@ -25,6 +25,10 @@ CASES = [
     ("rkdp-corr", {"solver": "rkdp", "correction": True}),
     ("rkdverk", {"solver": "rkdverk"}),
     ("rkf", {"solver": "rkf"}),
+    ("rkfeagin10", {"solver": "rkfeagin10"}),
+    ("rkfeagin10-corr", {"solver": "rkfeagin10", "correction": True}),
+    ("rkfeagin12", {"solver": "rkfeagin12"}),
+    ("rkfeagin14", {"solver": "rkfeagin14"}),
     ("rkgl", {"solver": "rkgl"}),
     ("rklc", {"solver": "rklc"}),
     ("trapeze2", {"solver": "trapeze", "refine_steps_count": 2}),
