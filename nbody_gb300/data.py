@@ -1,8 +1,8 @@
 """Body data: the host-side counterpart of the reference's `nbody_data`.
 
-Mirrors nbody/nbody_data.h (bodies, time, step, load/save, make_universe)
-and adds the seeded synthetic inputs the GB300 engine is measured on
-(uniform cube, Plummer sphere).  Everything here is input preparation on the
+Mirrors nbody/nbody_data.h (bodies, time, step, the G1 table load/save of
+the reference's golden vectors, make_universe) and adds the seeded synthetic
+inputs the GB300 engine is measured on (uniform cube, Plummer sphere).  Everything here is input preparation on the
 host; forces and conservation sums run on the GPU through the engine.
 """
 from __future__ import annotations
@@ -15,14 +15,6 @@ import numpy as np
 MIN_DISTANCE = 1e-8  # nbody/nbtype.h:79, compared with r^2
 BLOCK_SIZE = 64      # nbody/nbtype.h:77 NBODY_DATA_BLOCK_SIZE
 
-# Mass factors of the loader's unit systems (nbody/nbtype.h:79-85 and
-# nbody/nbody_data.cpp:661-673): G in m^3/(kg s^2) (the CODATA 1986 value the
-# reference uses), and the same G in au^3/(kg day^2) with the IAU astronomical
-# unit and the Julian day, evaluated in the reference's order.
-G_SI = 6.67259e-11
-AU_M = 149597870700.0
-DAY_S = 86400.0
-MASS_FACTOR = {"G1": 1.0, "SI": G_SI, "ADK": (G_SI * DAY_S * DAY_S) / (AU_M * AU_M * AU_M)}
 
 
 @dataclass
@@ -148,13 +140,11 @@ class NBodyData:
 
     # -- text I/O: nbody/nbody_data.cpp:417-651 -------------------------------
     @classmethod
-    def load(cls, path: str, units: str = "G1") -> "NBodyData":
-        """Text format 'X Y Z Vx Vy Vz Mass [Radius] ...', '//' comments
-        (nbody/nbody_data.cpp:442-512); masses are multiplied by the unit
-        system's factor (G1: 1, SI or ADK: the gravitational constant in
-        those units, nbody/nbody_data.cpp:661-673).  A malformed line raises
-        ValueError where the reference returns false."""
-        factor = MASS_FACTOR[units.upper()]
+    def load(cls, path: str) -> "NBodyData":
+        """The G1 table 'X Y Z Vx Vy Vz Mass [Radius] ...' with '//' comments
+        (nbody/nbody_data.cpp:442-512), the format of the reference's golden
+        vectors.  A malformed line raises ValueError where the reference
+        returns false."""
         rows = []
         with open(path) as fh:
             for line_n, line in enumerate(fh):
@@ -171,60 +161,9 @@ class NBodyData:
                 rows.append(vals)
         a = np.array(rows, dtype=np.float64).reshape(-1, 8)
         d = cls(vertices=a[:, 0:3].copy(), velocities=a[:, 3:6].copy(),
-                mass=a[:, 6] * factor, radius=a[:, 7].copy())
+                mass=a[:, 6].copy(), radius=a[:, 7].copy())
         # nbody/nbody_data.cpp:640-651 (load_initial box size)
         r = np.maximum(np.max(a[:, 0:3], axis=0) if len(a) else 1.0, 1.0)
-        d.box_size = int(np.max(r))
-        return d
-
-    @classmethod
-    def load_zeno_ascii(cls, path: str) -> "NBodyData":
-        """Zeno ASCII snapshot (nbody/nbody_data.cpp:514-614): the body count,
-        the dimension (3), one skipped line, then N masses, N positions and N
-        velocities, one per line.  Box size 1.  A malformed file raises
-        ValueError where the reference returns false."""
-        with open(path) as fh:
-            lines = fh.read().split("\n")
-        try:
-            count = int(lines[0].strip())
-            dim = int(lines[1].strip())
-        except (IndexError, ValueError) as exc:
-            raise ValueError(f"{path}: no body count or dimension") from exc
-        if dim != 3:
-            raise ValueError(f"{path}: dimension {dim}, not 3")
-        if len(lines) < 3 or not lines[2]:
-            raise ValueError(f"{path}: missing line 3")
-        body = lines[3:]
-        if len(body) < 3 * count or any(not body[k].strip() for k in range(3 * count)):
-            raise ValueError(f"{path}: unexpected end of data")
-        mass = np.array([float(body[k]) for k in range(count)])
-
-        def vectors(first):
-            out = np.zeros((count, 3))
-            for k in range(count):
-                cols = body[first + k].split()
-                if len(cols) != 3:
-                    raise ValueError(f"{path}: invalid vector {cols}")
-                out[k] = [float(c) for c in cols]
-            return out
-
-        d = cls(vertices=vectors(count), velocities=vectors(2 * count), mass=mass,
-                radius=np.zeros(count))
-        d.box_size = 1
-        return d
-
-    @classmethod
-    def load_initial(cls, path: str, kind: str) -> "NBodyData":
-        """nbody/nbody_data.cpp:616-659: 'Zeno', 'G1', 'SI' or 'ADK' (case
-        blind); the box size is then the largest coordinate, at least 1."""
-        k = kind.upper()
-        if k == "ZENO":
-            d = cls.load_zeno_ascii(path)
-        elif k in MASS_FACTOR:
-            d = cls.load(path, k)
-        else:
-            raise ValueError("unknown initial state type; possible values are Zeno, G1, SI, ADK")
-        r = np.maximum(np.max(d.vertices, axis=0), 1.0) if d.get_count() else np.ones(3)
         d.box_size = int(np.max(r))
         return d
 

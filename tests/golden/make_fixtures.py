@@ -3,9 +3,9 @@
 The reference (drons/nbody) pins its solvers with 16-body end states after
 t = 0.3 (test/solver/test_nbody_solver.cpp:43-145): the initial state
 test/data/initial_state.txt and one end state per solver, compared at 1e-12
-absolute.  Its data loaders are pinned with a Zeno ASCII snapshot, the same
-bodies as a table, and three malformed tables.  The GPU machine has no copy of the reference, so the files travel with
-the tests.  Run from the repository root:
+absolute.  Its table loader is pinned with three malformed tables.  The
+reference is not on the machine the GPU tests run on, so the files travel
+with the tests.  Run from the repository root:
 
     python tests/golden/make_fixtures.py /path/to/reference
 """
@@ -17,8 +17,8 @@ FILES = ["initial_state", "euler", "rk4", "rkdp", "rkdp-corr", "rkck", "rkf",
          "midpoint", "rkdverk", "rkfeagin10", "rkfeagin12", "rkfeagin14",
          "rkgl", "rklc", "adams5", "adams5-corr", "bulirsch-stoer",
          "midpoint-st", "rkfeagin10-corr", "trapeze2",
-         # the loaders' fixtures (test/stream/test_nbody_stream.cpp:344-372)
-         "zeno_ascii", "zeno_table", "inv_column", "inv_columns_count", "inv_radius"]
+         # the table loader's fixtures (test/stream/test_nbody_stream.cpp:344-372)
+         "inv_column", "inv_columns_count", "inv_radius"]
 
 
 def main(ref_root: str) -> None:
@@ -30,4 +30,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python tests/golden/make_fixtures.py /path/to/reference")
+    main(sys.argv[1])
