@@ -10,17 +10,21 @@ One step = one rk4 step through the engine interface (4 fcompute + 3 fmadd
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 --impl reference times the reference's CPU implementation of the same path
-(the block engine restated in oracle/, all host threads) on a bounded sample
-of rows of the same workload; it runs on rank 0 only.
+(the block engine restated in oracle/, all host threads) over whole steps of
+the same workload (one Euler step = one full fcompute, the reference bench's
+step); it runs on rank 0 only.
 
 Multi-GPU: the path is run as independent replicas (one per rank); value is
 the sum over ranks of the pairs processed divided by the slowest rank's time.
 
-Rank 0 also runs, outside the timed region, and adds to the same line:
+Output: ONE JSON line on stdout, the last, a few KB: the headline plus
+summaries (bh_summary, ensemble_summary).  Rank 0 also runs, outside the
+timed region, the suites those summaries come from, and writes them in full
+to --suites-out (default bench_out/suites.json):
   bh          the Barnes-Hut suite at N = 2^20 (both trees, monopole and
               quadrupole cells, the coherent and the FP64 walks, refit, the
-              learned correction, the accuracy frontier, the rkdp run);
-  bh_summary  the suite's figures of the headline metric;
+              learned correction with its judge, the accuracy frontier, the
+              rkdp run);
   ensemble    2048 Plummer clusters stepped by the device-side rkdp;
   statistics  P, L, E, V of one state on the GPU against the host sums.
     python bench.py --bh-only [--bh-n N] [--bh-cases a,b]   the suite alone
@@ -65,6 +69,8 @@ def parse():
     ap.add_argument("--bh-cases", default="",
                     help="with --bh-only: comma-separated names of the suite's cases to run "
                          "(e.g. hilbert_theta_0.5); default all")
+    ap.add_argument("--suites-out", default="bench_out/suites.json",
+                    help="file for the full Barnes-Hut, ensemble and statistics results")
     return ap.parse_args()
 
 
@@ -191,37 +197,55 @@ def cpu_pairs_per_s(y, mass, target_s: float, threads: int):
 
 
 def run_reference(args):
-    rank, _, world = int(os.environ.get("RANK", "0")), 0, int(os.environ.get("WORLD_SIZE", "1"))
+    """The reference's fastest CPU direct engine (block, nbody/nbody_engine_block.cpp:
+    14-126, restated in the oracle) on all host threads, timed over whole
+    steps of the reference bench's own kind: one Euler step = one full
+    fcompute over all N rows and bodies plus y += dt f (test/bench/bench.h:115
+    reports wall time / steps of exactly this)."""
+    rank, world = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
     from nbody_gb300.data import NBodyData
+    from oracle.oracle import load_oracle
+    orc = load_oracle()
     threads = os.cpu_count() or 1
-    d = NBodyData.plummer(args.n, seed=1)
+    n = args.n
+    d = NBodyData.plummer(n, seed=1)
     y, mass = d.to_state(), d.mass
-    vals = []
-    rows_used = 0
+    f = np.zeros_like(y)
+    step_s = []
     t_start = time.perf_counter()
     for k in range(args.warmup + args.steps):
-        v, rows_used, _ = cpu_pairs_per_s(y, mass, 3.0, threads)
+        t0 = time.perf_counter()
+        orc.fcompute_block_range(y, mass, f, 0, n, threads)
+        y += DT * f  # the Euler step's fmadd_inplace(y, f, dt)
         if k >= args.warmup:
-            vals.append(v)
-    value = float(np.mean(vals))
-    per_step_ms = 4.0 * args.n * args.n / value * 1e3
+            step_s.append(time.perf_counter() - t0)
+    wall = time.perf_counter() - t_start
+    mean_s = float(np.mean(step_s))
+    value = float(n) * n / mean_s
     line = {
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step_ms,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_s * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": WORKLOAD, "n": args.n,
-                   "precision": "f64 pairs and state (the reference's block engine), "
-                                "reference clamp r^2 >= 1e-8 instead of softening",
-                   "cpu": "block engine (nbody/nbody_engine_block.cpp) restated in oracle/, "
-                          "OpenMP over host cores; the reference itself needs Qt (absent)"},
+        "config": {"workload": WORKLOAD, "n": n,
+                   "step": "one Euler step (1 full fcompute: N^2 pairs, all rows; + y += dt f), "
+                           "the reference bench's step",
+                   "differs_from_gb300_arm": [
+                       "f64 pair arithmetic (the block engine) instead of f32 pairs + two-sum",
+                       "the reference's clamp r^2 >= 1e-8, no softening (the block engine "
+                       "has none) instead of softening 1e-3",
+                       "Euler steps (1 fcompute) instead of rk4 steps (4 fcomputes); the "
+                       "metric counts pairs either way"],
+                   "cpu": "block engine restated in oracle/ (OpenMP over all host threads); "
+                          "the reference's own build needs Qt, absent on this host"},
         "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
-                         "sample": f"{rows_used} of {args.n} rows x {args.n} bodies per step"},
+                         "sample": f"whole steps: {args.steps} timed Euler steps of the full "
+                                   f"{n}-body workload after {args.warmup} warm-up steps"},
         "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
-        "wall_s": time.perf_counter() - t_start,
+        "wall_s": wall,
     }
     print(json.dumps(line), flush=True)
 
@@ -245,11 +269,14 @@ def read_traffic():
 
 def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 5, walk: int = 1,
              weights=None, order: int = 1, build_rate: int = 0, build: int = 2,
-             precision: str = "mixed", tune=None):
+             precision: str = "mixed", tune=None, judge: bool = True):
     """Barnes-Hut fcompute (tree rebuilt every call) at opening ratio lam.
     walk 1 = group walk with interaction lists, 0 = warp-coherent stackless;
     build 0 = the reference's kd-median tree, 1 Morton, 2 Hilbert order;
-    precision "fp64" = the reference's per-body walk and arithmetic."""
+    precision "fp64" = the reference's per-body walk and arithmetic.
+    learned: every timed call is a new engine step, so each is judged (a
+    sampled direct sum) and falls back to plain theta = 0.5 when the judge
+    finds the learned p99 larger; judge False times the learned walk alone."""
     from nbody_gb300 import _lib
     from nbody_gb300.engine import create_engine
     e = create_engine({"engine": "gb300", "algo": "bh", "precision": precision,
@@ -267,6 +294,8 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
         return {"unavailable": "engine init failed"}
     if weights is not None:
         e.learn_set_weights(weights)
+    if learned:
+        e.tune_set("learned.judge", int(judge))
     f = e.create_buffer(8 * 6 * n_bh)
     step = 0
     for _ in range(2):
@@ -285,13 +314,16 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
     wall = (time.perf_counter() - t0) / calls
     tb, nb = e.profile_query(_lib.K_TREE_BUILD)
     tw, nw = e.profile_query(_lib.K_BH_WALK)
+    tj, nj = e.profile_query(_lib.K_JUDGE)
+    band_rows = e.learn_band_rows() if learned else 0
     visits, inter = e.bh_counters()
+    jst = e.learn_judge_stats() if learned else None
     out = np.zeros(6 * n_bh)
     e.read_buffer(out, f)
     a = out[3 * n_bh:].reshape(3, n_bh).T[rows]
     rel = np.linalg.norm(a - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
     e.close()
-    ms = (tb + tw) / calls
+    ms = (tb + tw + tj) / calls
     # node records read by the walk (20 B each: com.xyz + crit^2, mass), per
     # warp test, plus the body rows (16 B in, 24 B out)
     walk_bytes = visits / calls * 20.0 + n_bh * 40.0
@@ -305,46 +337,86 @@ def bench_bh(n_bh: int, lam: float, learned: bool, rows, a_ref, d, calls: int = 
             "build_ms": tb / calls, "walk_ms": tw / max(nw, 1),
             "p50": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99)),
             "interactions_per_body": inter / calls / n_bh,
-            "warp_node_visits_per_warp": visits / calls / (n_bh / 32)}
+            "warp_node_visits_per_warp": visits / calls / (n_bh / 32),
+            **({"node_visits_per_body": visits / calls / n_bh} if precision == "fp64" else {}),
+            **({"judge_ms": tj / calls, "judge": jst} if learned and judge else {}),
+            **({"band_rows_per_body": band_rows / calls / n_bh} if learned else {})}
 
 
-def bh_rkdp_run(n_bh: int, d, advises: int = 5, dt: float = 1e-3):
-    """The 2^20-body Barnes-Hut run as the reference would drive it: the rkdp solver
-    (nbody/nbody_solver_rk_butcher.cpp, error threshold 1e-6 on the unscaled
-    max |sum (b2 - b1) k|) driving the Barnes-Hut engine (theta 0.5, tree
-    rebuilt every fcompute) for `advises` advise calls.  The embedded error of
-    FP32 Barnes-Hut forces has a floor near 1e-4 whatever the step, so every
-    step subdivides once (max_recursion 1, 8 substeps) and is accepted at the
-    cap; reported: wall time, fcompute calls, errors seen."""
+def fp64_two_galaxies(n_bh: int):
+    """The FP64 parity walk (the reference's kd tree, per-body walk and
+    arithmetic) at theta 0.5 on nbody_data::make_universe(n/2): the input of
+    the reference bench (test/bench/bench.h:60-63) its published times use.
+    Error against the FP64 direct sum on 4096 sampled bodies."""
+    from nbody_gb300.data import NBodyData
+    from oracle.oracle import load_oracle
+    d = NBodyData.make_universe(n_bh // 2)
+    rows = np.random.default_rng(8).choice(n_bh, size=4096, replace=False)
+    a_ref = load_oracle().accel_rows(d.to_state(), d.mass, 0.0, rows=rows)
+    r = bench_bh(n_bh, 2.0, False, rows, a_ref, d, calls=1, precision="fp64")
+    r["input"] = f"make_universe({n_bh // 2}): two galaxies of {n_bh // 2} bodies, no softening"
+    return r
+
+
+def bh_rkdp_run(n_bh: int, d, advises: int = 5, dt: float = 1e-3, max_recursion: int = 8,
+                refit_within_step: bool = True, max_calls: int = 3000):
+    """The 2^20-body Barnes-Hut run as the reference drives it: the rkdp solver
+    (nbody/nbody_solver_rk_butcher.cpp:163-248: error threshold 1e-6 on the
+    unscaled max |sum (b2 - b1) k|, the reference's default max_recursion 8
+    and 8 substeps) driving the Barnes-Hut engine at theta 0.5 for `advises`
+    advise calls.  The tree is built at the first fcompute of each advise and
+    refit for every other stage and substep of it (refit_within_step), so
+    the force field the embedded error sees is continuous; rebuilding at
+    every stage instead makes the error a floor of tree noise (1e-4 - 1e-3)
+    that no step size removes.  Reported: fcompute calls, bodies/s, the
+    errors of the accepted steps, whether the recursion cap was hit."""
     from nbody_gb300.data import NBodyData
     from nbody_gb300.engine import create_engine
     from nbody_gb300.solvers import create_solver
     dd = NBodyData(vertices=d.vertices.copy(), velocities=d.velocities.copy(), mass=d.mass.copy())
     e = create_engine({"engine": "gb300", "algo": "bh", "precision": "mixed",
                        "softening": SOFTENING, "distance_to_node_radius_ratio": 2.0,
-                       "tree_layout": "heap_stackless"})
+                       "tree_layout": "heap_stackless",
+                       "tree_refit_within_step": refit_within_step})
     e.init(dd)
-    s = create_solver({"solver": "rkdp", "error_threshold": 1e-6, "max_recursion": 1,
-                       "substep_subdivisions": 8})
+    s = create_solver({"solver": "rkdp", "error_threshold": 1e-6,
+                       "max_recursion": max_recursion, "substep_subdivisions": 8})
     s.set_time_step(1e-9, dt)
     s.set_engine(e)
     calls = [0]
     fc = e.fcompute
 
+    class CallCap(Exception):
+        pass
+
     def counted(t, y, f):
+        # an error that never falls below the threshold recurses to the
+        # minimum step (8^7 substeps per advise): stop at a fixed budget
+        if calls[0] >= max_calls:
+            raise CallCap()
         calls[0] += 1
         return fc(t, y, f)
     e.fcompute = counted
     errs = []
+    aborted = False
     t0 = time.perf_counter()
-    for _ in range(advises):
-        s.advise(dt)
-        errs.append(s.last_error)
+    try:
+        for _ in range(advises):
+            s.advise(dt)
+            errs.append(s.last_error)
+    except CallCap:
+        aborted = True
     e.synchronize()
     wall = time.perf_counter() - t0
     e.close()
-    return {"advises": advises, "dt": dt, "wall_s": wall, "fcompute_calls": calls[0],
+    return {"advises": len(errs), "advises_asked": advises, "aborted_at_call_budget": aborted,
+            "call_budget": max_calls, "dt": dt, "error_threshold": 1e-6,
+            "max_recursion": max_recursion, "refit_within_step": refit_within_step,
+            "wall_s": wall, "fcompute_calls": calls[0],
             "bodies_per_s": n_bh * calls[0] / wall, "last_errors": errs,
+            "accepted_substeps": s.accepted_steps,
+            "max_accepted_error": s.max_accepted_error if s.accepted_steps else None,
+            "hit_recursion_cap": s.capped_steps > 0,
             "t_end": dd.get_time()}
 
 
@@ -459,15 +531,25 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
     y = d.to_state()
     rows = np.random.default_rng(7).choice(n_bh, size=4096, replace=False)
     a_ref = load_oracle().accel_rows(y, d.mass, SOFTENING, rows=rows)
-    res = {"workload": f"Barnes-Hut fcompute, N={n_bh} Plummer, softening 1e-3, heap_stackless, "
+    res = {"n": n_bh,
+           "workload": f"Barnes-Hut fcompute, N={n_bh} Plummer, softening 1e-3, heap_stackless, "
                        "tree rebuilt every call, FP32 walk / FP64 state",
            "error_judge": "FP64 direct sum (oracle) on 4096 sampled bodies"}
 
+    learned_w = {}
+
     def learned_case():
         w, fit = train_correction()
+        learned_w["w"] = w
         r = bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=w)
         r["training"] = fit
         return r
+
+    def learned_raw_case():
+        if "w" not in learned_w:
+            learned_w["w"] = train_correction()[0]
+        return bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=learned_w["w"],
+                        judge=False)
 
     suite = {
         # the reference's kd-median tree at the reference's opening ratios,
@@ -491,6 +573,10 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
         # the FP64 parity path: the reference's tree, walk and arithmetic
         "fp64_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, calls=1,
                                            precision="fp64"),
+        # the same parity walk on the reference's own bench input (two
+        # galaxies, nbody_data::make_universe), where its published GPU
+        # times were measured: interactions per body on both inputs
+        "fp64_theta_0.5_two_galaxies": lambda: fp64_two_galaxies(n_bh),
         "coherent_walk_hilbert_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d,
                                                             walk=0),
         # the walk the learned correction extends (with its FP64 node
@@ -504,8 +590,14 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
         "refit_rate4_hilbert_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d,
                                                           calls=8, build_rate=4),
         "learned_theta_0.9": learned_case,
+        # the learned walk alone (no judge, no fallback)
+        "learned_walk_theta_0.9": learned_raw_case,
         "accuracy_frontier": lambda: accuracy_frontier(n_bh, rows, a_ref, d),
         "rkdp_theta_0.5": lambda: bh_rkdp_run(n_bh, d),
+        # the same run with a tree rebuilt at every stage (the reference's
+        # rule at tree_build_rate 0), recursion capped at one level
+        "rkdp_theta_0.5_rebuild_every_stage": lambda: bh_rkdp_run(
+            n_bh, d, max_recursion=1, refit_within_step=False),
     }
     for name, run in suite.items():
         if cases is None or name in cases:
@@ -513,32 +605,83 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
     # the learned walk against plain theta 0.5 on the same GPU: the default
     # (Hilbert tree, group walk) and the reference's tree
     for base in ("hilbert_theta_0.5", "plain_theta_0.5"):
-        if base in res and "learned_theta_0.9" in res:
-            p05, l09 = res[base], res["learned_theta_0.9"]
-            res[f"learned_0.9_vs_{base}"] = {
-                "bodies_per_s_ratio": l09["bodies_per_s"] / p05["bodies_per_s"],
-                "p99_ratio": l09["p99"] / p05["p99"]}
+        for lk in ("learned_theta_0.9", "learned_walk_theta_0.9"):
+            if base in res and lk in res:
+                p05, l09 = res[base], res[lk]
+                tag = "learned_0.9" if lk == "learned_theta_0.9" else "learned_walk_0.9"
+                res[f"{tag}_vs_{base}"] = {
+                    "bodies_per_s_ratio": l09["bodies_per_s"] / p05["bodies_per_s"],
+                    "p99_ratio": l09["p99"] / p05["p99"]}
     return res
+
+
+def _r(x, digits: int = 4):
+    """A float rounded to `digits` significant digits (keeps the headline short)."""
+    if x is None or not isinstance(x, float) or not np.isfinite(x) or x == 0.0:
+        return x
+    return float(f"{x:.{digits}g}")
+
+
+def write_suites(path: str, suites: dict):
+    """The full Barnes-Hut, ensemble and statistics results go to a file (the
+    headline line carries their summaries); returns the path written."""
+    try:
+        p = Path(path)
+        p.parent.mkdir(parents=True, exist_ok=True)
+        p.write_text(json.dumps(suites, indent=1, default=float))
+        return str(p)
+    except OSError as exc:
+        print(f"bench: could not write {path}: {exc}", file=sys.stderr)
+        return None
 
 
 def bh_summary(bh):
     """The Barnes-Hut figures of the headline metric, picked from the suite:
-    bodies/s at p99 <= 1e-4 (and 1e-2, 1e-3) and theta = 0.5 on both trees."""
+    bodies/s at p99 <= 1e-4 (and 1e-2, 1e-3), theta = 0.5 on both trees, the
+    learned theta = 0.9 walk with its judge, and the learned ratios."""
     if not bh:
         return None
-    out = {}
+    out = {"n": bh.get("n")}
     fr = bh.get("accuracy_frontier")
     if fr:
         for tgt, b in fr["best"].items():
             if b["best"]:
-                out[f"p99_le_{tgt}"] = {"path": b["best"]["path"], "ms": b["best"]["ms"],
-                                        "bodies_per_s": b["bodies_per_s"],
+                out[f"p99_le_{tgt}"] = {"path": b["best"]["path"], "ms": _r(b["best"]["ms"]),
+                                        "p99": _r(b["best"]["p99"]),
+                                        "bodies_per_s": _r(b["bodies_per_s"]),
                                         "speedup_vs_reference_method":
-                                            b["speedup_vs_reference_method"]}
-    for k in ("hilbert_theta_0.5", "plain_theta_0.5", "learned_theta_0.9",
-              "coherent_walk_theta_0.9"):
+                                            _r(b["speedup_vs_reference_method"])}
+    for k in ("hilbert_theta_0.5", "plain_theta_0.5", "hilbert_theta_0.9", "learned_theta_0.9",
+              "learned_walk_theta_0.9", "fp64_theta_0.5"):
+        if k in bh and "bodies_per_s" in bh[k]:
+            out[k] = {x: _r(bh[k][x]) for x in ("ms_per_fcompute", "bodies_per_s", "p50", "p99")}
+            if "judge" in bh[k]:
+                out[k]["judge"] = bh[k]["judge"]
+    for k in ("learned_0.9_vs_hilbert_theta_0.5", "learned_0.9_vs_plain_theta_0.5",
+              "learned_walk_0.9_vs_hilbert_theta_0.5", "learned_walk_0.9_vs_plain_theta_0.5"):
         if k in bh:
-            out[k] = {x: bh[k][x] for x in ("ms_per_fcompute", "bodies_per_s", "p50", "p99")}
+            out[k] = {x: _r(v) for x, v in bh[k].items()}
+    if "rkdp_theta_0.5" in bh:
+        r = bh["rkdp_theta_0.5"]
+        out["rkdp_theta_0.5"] = {x: _r(r[x]) if isinstance(r[x], float) else r[x]
+                                 for x in ("advises", "aborted_at_call_budget",
+                                           "fcompute_calls", "bodies_per_s",
+                                           "max_recursion", "error_threshold",
+                                           "accepted_substeps", "max_accepted_error",
+                                           "hit_recursion_cap")
+                                 if x in r}
+    return out
+
+
+def ensemble_summary(ens):
+    """The ensemble figures without the autotuner's table."""
+    if not ens:
+        return None
+    keep = ("system_steps_per_s", "accepted_fraction", "ms_per_step", "pairs_per_s",
+            "fp32_fraction", "energy_drift_median", "energy_drift_max")
+    out = {k: _r(ens[k]) for k in keep if k in ens}
+    out["bodies"] = ens.get("bodies")
+    out["tile"] = ens.get("autotuner", {}).get("best")
     return out
 
 
@@ -736,6 +879,9 @@ def run_gb300(args):
     stats = run_stats_bench(n) if (rank == 0 and not args.no_ensemble) else None
 
     if rank == 0:
+        suites = {"bh": bh, "statistics": stats, "ensemble": ensemble,
+                  "direct_tuning": tuning}
+        suites_path = write_suites(args.suites_out, suites)
         line = {
             "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -746,18 +892,16 @@ def run_gb300(args):
                        "l2": "flushed between timed steps (256 MB write)",
                        "parallelism": f"replicas x{world}",
                        "tuning": tuning["best"]},
-            "roofline": {"bound": "fp32", "achieved": achieved_tflops,
-                         "peak": peak_flops / 1e12, "unit": "TFLOP/s",
-                         "frac": achieved_tflops / (peak_flops / 1e12),
+            "roofline": {"bound": "fp32", "achieved": _r(achieved_tflops),
+                         "peak": _r(peak_flops / 1e12), "unit": "TFLOP/s",
+                         "frac": _r(achieved_tflops / (peak_flops / 1e12)),
                          "peak_note": "measured FFMA probe on this GPU (no FP32 entry in "
                                       "MEASURED_PEAKS.json); nominal %.1f TFLOP/s at 2070 MHz"
                                       % (nominal / 1e12),
-                         "frac_of_nominal": achieved_tflops * 1e12 / nominal,
+                         "frac_of_nominal": _r(achieved_tflops * 1e12 / nominal),
                          "kernel": "direct_sym_kernel",
                          "pairs_evaluated": pairs_evaluated,
-                         "note": "each unordered pair evaluated once and applied to both "
-                                 "bodies; achieved counts N^2 ordered pairs x 20 FLOP",
-                         "kernel_ms": k_avg_s * 1e3,
+                         "kernel_ms": _r(k_avg_s * 1e3),
                          "flop_per_pair": FLOP_PER_PAIR,
                          "traffic": read_traffic()},
             "cpu_baseline": cpu,
@@ -767,12 +911,12 @@ def run_gb300(args):
             "clocks": clk,
             "force_error": err,
             "bh_summary": bh_summary(bh),
-            "bh": bh,
-            "statistics": stats,
-            "ensemble": ensemble,
-            "wall_s_timed": wall,
+            "ensemble_summary": ensemble_summary(ensemble),
+            "suites_file": suites_path,
+            "wall_s_timed": _r(wall),
         }
-        print(json.dumps(line), flush=True)
+        # the headline is the last stdout line, kept to a few KB
+        print(json.dumps(line, separators=(",", ":")), flush=True)
     e.free_buffer(flush)
     e.close()
     if world > 1:

@@ -159,6 +159,7 @@ enum nbg_kernel_id {
     NBG_K_BH_WALK = 2,    /* Barnes-Hut traversal kernel */
     NBG_K_VECOPS = 3,     /* buffer algebra kernels */
     NBG_K_ENS_STEP = 4,   /* one whole ensemble RK step (graph launch) */
+    NBG_K_JUDGE = 5,      /* the learned path's per-step judge */
     NBG_K_COUNT = 8
 };
 /* Enable CUDA-event timing of each kernel class on the engine stream. */
@@ -197,7 +198,16 @@ nbg_status nbg_bh_fallback_groups(nbg_engine* e, uint64_t* groups);
  * nbg_params.learned = 1 (Barnes-Hut, mixed precision); tuning keys:
  * "learned.group" one sample per (body, cell) (0, default) or per (warp,
  * cell) at the warp centroid (1); "learned.weighted" (0 default, 1: training
- * loss weighted by the cell's force scale (m / s^2)^2). */
+ * loss weighted by the cell's force scale (m / s^2)^2).
+ * Judge and fallback: at the first fcompute of every engine step a direct
+ * sum on a seeded sample of bodies ("learned.judge_samples", default 4096,
+ * rounded down to a power of two; "learned.judge_seed", default 1) measures
+ * the relative force error of the learned walk and of the plain walk at the
+ * tight ratio learned_tight_ratio (theta = 0.5 by default) on the same
+ * bodies; when the learned p99 is the larger, the plain walk (the engine's
+ * Barnes-Hut path without the correction, tree rebuilt at the tight ratio)
+ * computes that fcompute and every other fcompute of the step.
+ * "learned.judge" = 0 turns the judge and the fallback off. */
 size_t nbg_learn_param_count(void);
 nbg_status nbg_learn_set_weights(nbg_engine* e, const float* w, size_t count);
 nbg_status nbg_learn_get_weights(nbg_engine* e, float* w, size_t count);
@@ -227,6 +237,18 @@ nbg_status nbg_learn_loss_grad(nbg_engine* e, const float* x, const float* t, si
 /* Network outputs g (x [count][16] -> out [count][3]) with the inference
  * routine of the walk. */
 nbg_status nbg_learn_predict(nbg_engine* e, const float* x, size_t count, float* out);
+/* The judge's figures: out[0] engine step judged last, [1] p50 and [2] p99
+ * relative error of the learned forces, [3] p50 and [4] p99 of the plain
+ * walk at the tight ratio, [5] RMS learned, [6] RMS plain, [7] 1 when that
+ * step ran the plain walk, [8] sampled bodies, [9] steps judged and [10]
+ * steps that fell back since the engine was created.  All zero before the
+ * first judged step.  count >= NBG_JUDGE_STATS. */
+#define NBG_JUDGE_STATS 11
+nbg_status nbg_learn_judge_stats(nbg_engine* e, double* out, size_t count);
+/* Network rows the learned walk evaluated for band interactions (one per
+ * body-cell pair, or per warp-cell pair with "learned.group" = 1) since the
+ * last nbg_bh_counters call, which resets it. */
+nbg_status nbg_learn_band_rows(nbg_engine* e, uint64_t* rows);
 /* Body index of each leaf of the last tree (leaf order), [N]. */
 nbg_status nbg_tree_leaves(nbg_engine* e, int* body_of_leaf);
 
@@ -269,7 +291,12 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       per four groups),
  *       "bh.eval_unroll" (1, 2 or 4: unroll of the interaction-list loop of
  *       the 64-body walk, at 5 CTAs per SM with shared-memory accumulators
- *       or at 4 with register accumulators)). */
+ *       or at 4 with register accumulators),
+ *       "bh.refit_within_step" (0, the default: the reference's rule, a full
+ *       build when tree_build_rate is 0 or step % rate == 0; 1: a full
+ *       build at the first fcompute of each engine step and refits of that
+ *       topology for the step's other stages, so the force field is
+ *       continuous within one solver step)). */
 nbg_status nbg_tune_set(nbg_engine* e, const char* key, int64_t value);
 nbg_status nbg_tune_get(nbg_engine* e, const char* key, int64_t* value);
 
@@ -295,9 +322,15 @@ nbg_status nbg_autotune(nbg_engine* e, int reps, char* report, size_t report_len
  * that loads it until the process exits, which caps n at
  * NBG_NOALLOC_MAX_BODIES (larger n returns NBG_ERR_TOO_LARGE and touches
  * nothing).  The first call on a device looks up that array's device address
- * (one-time set-up, with that device current).  Returns after f holds the
- * result.  All calls share the one array: calls that overlap on the GPU
- * (from several host threads or streams) race and must be serialised. */
+ * (one-time set-up, with that device current).  Under CUDA's lazy module
+ * loading (the default) the array and the kernel's code are placed on a GPU
+ * when the library's direct-sum code is first used there, so when this call
+ * is that first use, the CUDA driver loads the module inside it (its own
+ * allocation, done once); a caller that must see no allocation at all in its
+ * loop makes one call during set-up, or sets CUDA_MODULE_LOADING=EAGER.
+ * Returns after f holds the result (the error word is read on `stream`).
+ * All calls share the one array: calls that overlap on the GPU (from
+ * several host threads or streams) race and must be serialised. */
 #define NBG_NOALLOC_MAX_BODIES 131072
 nbg_status nbg_direct_mixed_noalloc(const double* y, const double* mass, double* f,
                                     size_t n, double softening, void* stream);

@@ -20,7 +20,8 @@ ALGO = {"direct": 0, "bh": 1}
 PRECISION = {"fp64": 0, "mixed": 1}
 LAYOUT = {"heap": 1, "heap_stackless": 2}
 TRAVERSE = {"cycle": 0, "nested_tree": 1}
-K_DIRECT, K_TREE_BUILD, K_BH_WALK, K_VECOPS = 0, 1, 2, 3
+K_DIRECT, K_TREE_BUILD, K_BH_WALK, K_VECOPS, K_ENS_STEP, K_JUDGE = 0, 1, 2, 3, 4, 5
+JUDGE_STATS = 11  # NBG_JUDGE_STATS
 
 # Every symbol the header declares: checked by the CPU test suite.
 EXPORTS = [
@@ -44,7 +45,8 @@ EXPORTS = [
     "nbg_ensemble_launch_count", "nbg_ensemble_profile", "nbg_autotune",
     "nbg_ensemble_autotune", "nbg_stream_open", "nbg_stream_set_header", "nbg_stream_write",
     "nbg_stream_write_host", "nbg_stream_flush", "nbg_stream_close", "nbg_stream_last_error",
-    "nbg_bh_stack_peak", "nbg_bh_fallback_groups",
+    "nbg_bh_stack_peak", "nbg_bh_fallback_groups", "nbg_learn_judge_stats",
+    "nbg_learn_band_rows",
 ]
 
 
@@ -161,6 +163,8 @@ def load() -> C.CDLL:
     _proto(lib, "nbg_learn_loss_grad", i32, vp, fp, fp, sz, dp, fp)
     _proto(lib, "nbg_tree_leaves", i32, vp, ip)
     _proto(lib, "nbg_learn_predict", i32, vp, fp, sz, fp)
+    _proto(lib, "nbg_learn_judge_stats", i32, vp, dp, sz)
+    _proto(lib, "nbg_learn_band_rows", i32, vp, C.POINTER(u64))
     _proto(lib, "nbg_statistics", i32, vp, vp, dp)
     u32p = C.POINTER(C.c_uint32)
     _proto(lib, "nbg_ensemble_params_default", None, C.POINTER(EnsembleParams))

@@ -227,6 +227,7 @@ void nbg_engine_destroy(nbg_engine* e) {
     if (e->stream) cudaStreamSynchronize(e->stream);
     tree_destroy(e);
     learn_destroy(e);
+    judge_destroy(e);
     for (const nbg_buffer* b : e->buffers) {
         cudaFree(b->dptr);
         delete b;

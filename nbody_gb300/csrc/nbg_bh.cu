@@ -36,8 +36,8 @@
 
 namespace nbg {
 
-nbg_status learned_walk(nbg_engine* e, const double* y, double* f);  // nbg_learned.cu
-bool learned_ready(const nbg_engine* e);
+// nbg_learned.cu: the learned path's fcompute (learned walk, judge, fallback)
+nbg_status learned_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f);
 
 namespace {
 
@@ -71,6 +71,7 @@ __global__ void bh_walk_fp64_kernel(const double* __restrict__ y, const double* 
     double fx = 0.0, fy = 0.0, fz = 0.0;
     int curr = 1;
     long long steps = 0;
+    unsigned inter = 0;
     do {
         const double dx = __dsub_rn(v1[0], t.com[curr]);
         const double dy = __dsub_rn(v1[1], t.com[sz + curr]);
@@ -83,6 +84,7 @@ __global__ void bh_walk_fp64_kernel(const double* __restrict__ y, const double* 
             fy = __dadd_rn(fy, __dmul_rn(dy, c));
             fz = __dadd_rn(fz, __dmul_rn(dz, c));
             curr = next_down(curr);
+            ++inter;
         } else {
             curr = (2 * (size_t)curr < sz) ? 2 * curr : next_down(curr);
         }
@@ -91,6 +93,15 @@ __global__ void bh_walk_fp64_kernel(const double* __restrict__ y, const double* 
             break;
         }
     } while (curr != 1);
+    // node visits and interactions of this thread's body, one atomic per
+    // group of converged threads
+    const unsigned mask = __activemask();
+    const unsigned vis = __reduce_add_sync(mask, (unsigned)steps);
+    const unsigned itr = __reduce_add_sync(mask, inter);
+    if ((threadIdx.x & 31) == __ffs(mask) - 1) {
+        atomicAdd(&t.counters[0], (unsigned long long)vis);
+        atomicAdd(&t.counters[1], (unsigned long long)itr);
+    }
     f[b] = y[3 * n + b];
     f[n + b] = y[4 * n + b];
     f[2 * n + b] = y[5 * n + b];
@@ -854,23 +865,45 @@ nbg_status tree_quadrupoles(nbg_engine* e) {
 
 }  // namespace
 
+nbg_status bh_tree(nbg_engine* e, uint64_t step, const double* y, bool fp64_nodes, double lambda) {
+    const TreeState* t = e->tree;
+    bool build;
+    if (t == nullptr || !t->built || (fp64_nodes && t->f32))
+        build = true;
+    else if (e->tune_get("bh.refit_within_step", 0) != 0)
+        build = step != t->built_step;
+    else {
+        const uint64_t rate = e->params.tree_build_rate;
+        build = rate == 0 || step % rate == 0;
+    }
+    nbg_status s = build ? tree_build(e, y, fp64_nodes, lambda) : tree_refit(e, y, lambda);
+    if (s == NBG_OK && build) e->tree->built_step = step;
+    return s;
+}
+
 nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f) {
     const int n = (int)e->count;
-    const uint64_t rate = e->params.tree_build_rate;
-    const bool build = e->tree == nullptr || !e->tree->built || rate == 0 || step % rate == 0;
-    nbg_status s = build ? tree_build(e, y, e->params.precision == NBG_PREC_FP64 || e->params.learned)
-                         : tree_refit(e, y);
-    if (s != NBG_OK) return s;
-    TreeState* t = e->tree;
-    ProfScope ps(e, NBG_K_BH_WALK);
+    const double lambda = e->params.distance_to_node_radius_ratio;
     if (e->params.precision == NBG_PREC_FP64) {
+        nbg_status s = bh_tree(e, step, y, true, lambda);
+        if (s != NBG_OK) return s;
+        ProfScope ps(e, NBG_K_BH_WALK);
         bh_walk_fp64_kernel<<<(n + 127) / 128, 128, 0, e->stream>>>(
-            y, e->d_mass, f, n, e->params.traverse_type == NBG_TRAVERSE_NESTED_TREE ? 1 : 0, *t,
-            e->d_err);
+            y, e->d_mass, f, n, e->params.traverse_type == NBG_TRAVERSE_NESTED_TREE ? 1 : 0,
+            *e->tree, e->d_err);
         NBG_LAUNCHED(e, "bh_walk_fp64_kernel");
         return NBG_OK;
     }
-    if (e->params.learned) return learned_walk(e, y, f);
+    if (e->params.learned) return learned_fcompute(e, step, y, f);
+    nbg_status s = bh_tree(e, step, y, false, lambda);
+    if (s != NBG_OK) return s;
+    return mixed_walk(e, y, f);
+}
+
+nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
+    const int n = (int)e->count;
+    TreeState* t = e->tree;
+    ProfScope ps(e, NBG_K_BH_WALK);
     const float eps2 = (float)(e->params.softening * e->params.softening);
     const bool clamp = !(e->params.softening > 0.0);
     if (e->tune_get("bh.walk", 1) == 1 && n >= 32) {
@@ -1001,7 +1034,7 @@ extern "C" nbg_status nbg_bh_counters(nbg_engine* e, uint64_t* visits, uint64_t*
     unsigned long long h[2] = {0, 0};
     NBG_CUDA(e, cudaMemcpyAsync(h, e->tree->counters, sizeof(h), cudaMemcpyDeviceToHost, e->stream));
     NBG_CUDA(e, cudaStreamSynchronize(e->stream));
-    NBG_CUDA(e, cudaMemsetAsync(e->tree->counters, 0, 4 * sizeof(unsigned long long), e->stream));
+    NBG_CUDA(e, cudaMemsetAsync(e->tree->counters, 0, 5 * sizeof(unsigned long long), e->stream));
     if (visits) *visits = h[0];
     if (interactions) *interactions = h[1];
     return NBG_OK;

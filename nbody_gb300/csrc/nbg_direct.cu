@@ -849,10 +849,14 @@ extern "C" nbg_status nbg_direct_mixed_noalloc(const double* y, const double* ma
     if (cudaGetLastError() != cudaSuccess) return NBG_ERR_CUDA;
 
     // Synchronous: the result is in f when this returns, and a device-side
-    // wait that timed out is reported here.
+    // wait that timed out is reported here.  The error word is read on the
+    // caller's stream, so the call waits for that stream only (a plain
+    // cudaMemcpy would go through the legacy default stream and wait for
+    // unrelated work on other blocking streams).
     unsigned err_host = 0;
-    if (cudaStreamSynchronize(st) != cudaSuccess ||
-        cudaMemcpy(&err_host, d.err, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    if (cudaMemcpyAsync(&err_host, d.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
         cudaGetLastError();
         return NBG_ERR_CUDA;
     }

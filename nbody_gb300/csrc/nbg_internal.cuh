@@ -27,6 +27,7 @@ enum DeviceError : unsigned {
 
 struct TreeState;   // nbg_tree.cu
 struct LearnState;  // nbg_learned.cu
+struct JudgeState;  // nbg_judge.cu
 
 }  // namespace nbg
 
@@ -63,6 +64,7 @@ struct nbg_engine {
     // Barnes-Hut state
     nbg::TreeState* tree = nullptr;
     nbg::LearnState* learn = nullptr;
+    nbg::JudgeState* judge = nullptr;
 
     // measurement
     bool profiling = false;
@@ -145,6 +147,20 @@ nbg_status direct_fcompute(nbg_engine* e, const double* y, double* f);
 nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f);
 void tree_destroy(nbg_engine* e);
 void learn_destroy(nbg_engine* e);  // nbg_learned.cu
+
+// nbg_judge.cu: the learned path's per-step judge on a sample of at most
+// kJudgeMax bodies (learned forces f and the plain walk at lambda_t against
+// a direct sum); synchronises the engine stream to read its figures back
+constexpr int kJudgeMax = 4096;
+struct JudgeResult {
+    double p50_learned = 0.0, p99_learned = 0.0, p50_plain = 0.0, p99_plain = 0.0;
+    double rms_learned = 0.0, rms_plain = 0.0;
+    bool use_plain = false;
+    int samples = 0;
+};
+nbg_status judge_learned(nbg_engine* e, uint64_t step, const double* f, double lam_l,
+                         double lam_t, JudgeResult* out);
+void judge_destroy(nbg_engine* e);
 
 // nbg_probe.cu
 nbg_status measure_fp32_peak(nbg_engine* e, double* flops);

@@ -56,6 +56,12 @@ struct LearnState {
     unsigned long long* pair_count = nullptr;
     double* mom = nullptr;   // [6][size] FP64 second moments of the current tree
     size_t mom_size = 0;
+    // per-step judge (nbg_judge.cu): the step judged last, the step sent to
+    // the plain walk, counts, the last figures
+    bool judged_valid = false, plain_valid = false;
+    uint64_t judged_step = 0, plain_step = 0;
+    uint64_t judged = 0, fallbacks = 0;
+    JudgeResult last;
 };
 
 namespace {
@@ -661,7 +667,7 @@ learned_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n,
     float ax = 0.f, ay = 0.f, az = 0.f;
     float gx = 0.f, gy = 0.f, gz = 0.f;  // group correction (same on every lane)
     int qn = 0;
-    unsigned visits = 0, inter = 0;
+    unsigned visits = 0, inter = 0, rows = 0;
     int curr = 1;
     const int sz = (int)t.size;
 
@@ -693,6 +699,7 @@ learned_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n,
         gx += corr[0];
         gy += corr[1];
         gz += corr[2];
+        if (lane == 0) rows += (unsigned)qn;  // one network row per queued cell
         qn = 0;
     };
 
@@ -734,6 +741,7 @@ learned_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n,
                         mlp::infer_warp(feat, cg, S.frag, S.bias, S.xs[warp], S.os[warp], lane);
                         apply_head(feat, cg, g);
                         if (band) {
+                            ++rows;
                             const float k = __ldg(&t.nodem[curr]) * inv_s * inv_s;
                             ax = fmaf(k, g[0], ax);
                             ay = fmaf(k, g[1], ay);
@@ -761,11 +769,15 @@ learned_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n,
         f[4 * n + b] = (double)(ay + gy);
         f[5 * n + b] = (double)(az + gz);
     }
-    if (!live) inter = 0;
-    for (int o = 16; o > 0; o >>= 1) inter += __shfl_xor_sync(0xffffffffu, inter, o);
+    if (!live) inter = rows = 0;
+    for (int o = 16; o > 0; o >>= 1) {
+        inter += __shfl_xor_sync(0xffffffffu, inter, o);
+        rows += __shfl_xor_sync(0xffffffffu, rows, o);
+    }
     if (lane == 0) {
         atomicAdd(&t.counters[0], (unsigned long long)visits);
         atomicAdd(&t.counters[1], (unsigned long long)inter);
+        atomicAdd(&t.counters[4], (unsigned long long)rows);
     }
 }
 
@@ -886,6 +898,52 @@ nbg_status learned_walk(nbg_engine* e, const double* y, double* f) {
     return NBG_OK;
 }
 
+// The learned path's fcompute.  The tree is built (or refit) at the loose
+// ratio lambda_l with FP64 nodes (the features need them) and the learned
+// walk writes f.  At the first fcompute of every engine step the judge
+// ("learned.judge" = 1, the default) compares the learned forces and the
+// plain walk's at the tight ratio lambda_t on a sampled direct sum; when the
+// learned p99 is the larger, the tree is rebuilt at lambda_t and the plain
+// mixed walk (the engine's non-learned Barnes-Hut path) rewrites f, and every
+// further fcompute of that step takes the plain path as well, so that one
+// solver step sees one force field.
+nbg_status learned_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f) {
+    if (!learned_ready(e))
+        return set_error(e, NBG_ERR_NOT_INITIALIZED,
+                         "learned correction enabled but no weights are loaded");
+    LearnState* L = e->learn;
+    const double lam_l = e->params.distance_to_node_radius_ratio;
+    const double lam_t = e->params.learned_tight_ratio;
+    const bool judge = e->tune_get("learned.judge", 1) != 0;
+    if (judge && L->plain_valid && L->plain_step == step) {
+        nbg_status s = bh_tree(e, step, y, true, lam_t);
+        if (s != NBG_OK) return s;
+        return mixed_walk(e, y, f);
+    }
+    nbg_status s = bh_tree(e, step, y, true, lam_l);
+    if (s != NBG_OK) return s;
+    {
+        ProfScope ps(e, NBG_K_BH_WALK);
+        s = learned_walk(e, y, f);
+    }
+    if (s != NBG_OK || !judge || (L->judged_valid && L->judged_step == step)) return s;
+    JudgeResult r;
+    s = judge_learned(e, step, f, lam_l, lam_t, &r);
+    if (s != NBG_OK) return s;
+    L->judged_valid = true;
+    L->judged_step = step;
+    L->judged++;
+    L->last = r;
+    if (!r.use_plain) return NBG_OK;
+    L->fallbacks++;
+    L->plain_valid = true;
+    L->plain_step = step;
+    s = tree_build(e, y, true, lam_t);
+    if (s != NBG_OK) return s;
+    e->tree->built_step = step;
+    return mixed_walk(e, y, f);
+}
+
 }  // namespace nbg
 
 using namespace nbg;
@@ -932,7 +990,7 @@ nbg_status nbg_learn_generate(nbg_engine* e, size_t max_samples, uint64_t seed,
     if (s != NBG_OK) return s;
     LearnState* L = e->learn;
     const double* y = static_cast<const double*>(e->y->dptr);
-    s = tree_build(e, y, true);
+    s = tree_build(e, y, true, e->params.distance_to_node_radius_ratio);
     if (s != NBG_OK) return s;
     s = tree_features(e);
     if (s != NBG_OK) return s;
@@ -1211,6 +1269,31 @@ nbg_status nbg_learn_predict(nbg_engine* e, const float* x, size_t count, float*
         for (int c = 0; c < 3; ++c) out[i * 3 + c] = tmp[i * 4 + c];
     cudaFree(dx);
     cudaFree(dout);
+    return NBG_OK;
+}
+
+nbg_status nbg_learn_judge_stats(nbg_engine* e, double* out, size_t count) {
+    if (e == nullptr || out == nullptr || count < NBG_JUDGE_STATS) return NBG_ERR_INVALID_ARG;
+    for (size_t k = 0; k < NBG_JUDGE_STATS; ++k) out[k] = 0.0;
+    const LearnState* L = e->learn;
+    if (L == nullptr || !L->judged_valid) return NBG_OK;
+    const JudgeResult& r = L->last;
+    const double v[NBG_JUDGE_STATS] = {
+        (double)L->judged_step, r.p50_learned, r.p99_learned, r.p50_plain, r.p99_plain,
+        r.rms_learned, r.rms_plain, r.use_plain ? 1.0 : 0.0, (double)r.samples,
+        (double)L->judged, (double)L->fallbacks};
+    for (size_t k = 0; k < NBG_JUDGE_STATS; ++k) out[k] = v[k];
+    return NBG_OK;
+}
+
+nbg_status nbg_learn_band_rows(nbg_engine* e, uint64_t* rows) {
+    if (e == nullptr || rows == nullptr) return NBG_ERR_INVALID_ARG;
+    if (e->tree == nullptr) return set_error(e, NBG_ERR_NOT_INITIALIZED, "no tree built yet");
+    unsigned long long h = 0;
+    NBG_CUDA(e, cudaMemcpyAsync(&h, e->tree->counters + 4, sizeof(h), cudaMemcpyDeviceToHost,
+                                e->stream));
+    NBG_CUDA(e, cudaStreamSynchronize(e->stream));
+    *rows = h;
     return NBG_OK;
 }
 

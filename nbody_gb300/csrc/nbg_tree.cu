@@ -565,14 +565,14 @@ nbg_status tree_alloc(nbg_engine* e) {
     NBG_TRY(alloc(e, &t->node4, sz));
     NBG_TRY(alloc(e, &t->nodem, sz));
     NBG_TRY(alloc(e, &t->box4, 2 * sz));
-    NBG_TRY(alloc(e, &t->counters, 4));
+    NBG_TRY(alloc(e, &t->counters, 5));
 #undef NBG_TRY
     // index 0 is unused; zero everything once so stray reads are defined
     NBG_CUDA(e, cudaMemsetAsync(t->node4, 0, sz * sizeof(float4), e->stream));
     NBG_CUDA(e, cudaMemsetAsync(t->nodem, 0, sz * sizeof(float), e->stream));
     NBG_CUDA(e, cudaMemsetAsync(t->crit2, 0, sz * sizeof(double), e->stream));
     NBG_CUDA(e, cudaMemsetAsync(t->body_n, 0, sz * sizeof(int), e->stream));
-    NBG_CUDA(e, cudaMemsetAsync(t->counters, 0, 4 * sizeof(unsigned long long), e->stream));
+    NBG_CUDA(e, cudaMemsetAsync(t->counters, 0, 5 * sizeof(unsigned long long), e->stream));
     return NBG_OK;
 }
 
@@ -645,7 +645,7 @@ void tree_destroy(nbg_engine* e) {
     e->tree = nullptr;
 }
 
-nbg_status tree_build(nbg_engine* e, const double* y, bool fp64_nodes) {
+nbg_status tree_build(nbg_engine* e, const double* y, bool fp64_nodes, double lambda) {
     const int n = (int)e->count;
     if (e->tree == nullptr) {
         e->tree = new TreeState();
@@ -661,7 +661,7 @@ nbg_status tree_build(nbg_engine* e, const double* y, bool fp64_nodes) {
         }
     }
     TreeState* t = e->tree;
-    t->lambda = e->params.distance_to_node_radius_ratio;
+    t->lambda = lambda;
     // "bh.fp64_nodes" = 1 keeps the FP64 node update in mixed precision
     t->f32 = !fp64_nodes && e->tune_get("bh.fp64_nodes", 0) == 0;
     ProfScope ps(e, NBG_K_TREE_BUILD);
@@ -753,10 +753,10 @@ nbg_status tree_build(nbg_engine* e, const double* y, bool fp64_nodes) {
     return NBG_OK;
 }
 
-nbg_status tree_refit(nbg_engine* e, const double* y) {
+nbg_status tree_refit(nbg_engine* e, const double* y, double lambda) {
     TreeState* t = e->tree;
     const int n = (int)e->count;
-    t->lambda = e->params.distance_to_node_radius_ratio;
+    t->lambda = lambda;
     ProfScope ps(e, NBG_K_TREE_BUILD);
     const unsigned g = grid_for(n, 256, (unsigned)e->sm_count * 8u);
     if (t->f32)

@@ -16,7 +16,8 @@ struct TreeState {
     int levels = 0;   // K = log2(n)
     bool built = false;
     int curve = 0;    // leaf order of the last build: 0 kd-median, 1 Morton, 2 Hilbert
-    double lambda = 0.0;
+    double lambda = 0.0;  // opening ratio the node records' crit2 were formed with
+    uint64_t built_step = 0;  // engine step of the last full build
 
     // build scratch
     uint64_t* keys[2] = {nullptr, nullptr};  // radix keys (ping-pong)
@@ -55,8 +56,9 @@ struct TreeState {
     float4* quad = nullptr;   // [2][size] or null
 
     // walk counters: node tests, interactions, deepest group-walk stack,
-    // groups handed to the per-body fallback walk
-    unsigned long long* counters = nullptr;  // [4]
+    // groups handed to the per-body fallback walk, learned-walk band rows
+    // (body-cell pairs the network corrected)
+    unsigned long long* counters = nullptr;  // [5]
 
     // group walks that exceed a node-test cap give up; their group ids go
     // to fb_list and a per-body walk computes those bodies (nbg_bh.cu).
@@ -75,8 +77,24 @@ constexpr int kPartTile = 2048;  // elements per partition tile (256 threads x 8
 // order (1) or the kd-median tree (0); a curve tree halves the ordered list
 // at every level (one sort, no partitions; a different tree).
 // fp64_nodes: form the FP64 node arrays (the FP64 walk, the learned
-// correction's features); otherwise only the FP32 records
-nbg_status tree_build(nbg_engine* e, const double* y, bool fp64_nodes);
-nbg_status tree_refit(nbg_engine* e, const double* y);  // fixed topology, new positions
+// correction's features); otherwise only the FP32 records.  lambda: the
+// opening ratio of the nodes' critical radii.
+nbg_status tree_build(nbg_engine* e, const double* y, bool fp64_nodes, double lambda);
+// fixed topology, new positions (and critical radii at lambda)
+nbg_status tree_refit(nbg_engine* e, const double* y, double lambda);
+
+// nbg_bh.cu.  The tree for one fcompute: a full build or a refit of the last
+// topology.  The reference's rule (nbody/nbody_engine_cuda_bh_tex.cpp:46-163)
+// builds when tree_build_rate is 0 or step % rate == 0 and refits otherwise.
+// With "bh.refit_within_step" = 1 the engine builds only at the first
+// fcompute of each engine step (the step number changes) and refits for the
+// other stages of that step, so that the force field stays continuous
+// within a solver step (the solver advances the step once per advise).  A
+// caller that needs the FP64 node arrays (fp64_nodes) gets a build when the
+// last one formed only the FP32 records.
+nbg_status bh_tree(nbg_engine* e, uint64_t step, const double* y, bool fp64_nodes, double lambda);
+// The plain mixed-precision walk over the current tree (group walk by
+// default, "bh.walk" = 0 the warp-coherent walk), writing all of f.
+nbg_status mixed_walk(nbg_engine* e, const double* y, double* f);
 
 }  // namespace nbg

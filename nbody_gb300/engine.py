@@ -112,11 +112,27 @@ def create_engine(param: dict) -> Optional["NbodyEngineGB300"]:
     p = _params_from(param)
     if p is None:
         return None
+    # engine keys that map to tuning knobs of the library
+    tune = {}
     try:
-        return NbodyEngineGB300(p)
+        if "tree_refit_within_step" in param:
+            tune["bh.refit_within_step"] = int(bool(param["tree_refit_within_step"]))
+        if "learned_judge" in param:
+            tune["learned.judge"] = int(bool(param["learned_judge"]))
+        if "learned_judge_samples" in param:
+            tune["learned.judge_samples"] = int(param["learned_judge_samples"])
+            if tune["learned.judge_samples"] < 1:
+                return None
+    except (TypeError, ValueError):
+        return None
+    try:
+        e = NbodyEngineGB300(p)
     except NbgError as err:
         log.warning("gb300 engine not created: %s", err)
         return None
+    for k, v in tune.items():
+        e.tune_set(k, v)
+    return e
 
 
 class NbodyEngineGB300:
@@ -518,6 +534,29 @@ class NbodyEngineGB300:
         self._check(self._lib.nbg_learn_predict(self._h, x.ctypes.data_as(fp), x.shape[0],
                                                 out.ctypes.data_as(fp)), "learn_predict")
         return out
+
+    def learn_judge_stats(self) -> dict:
+        """The learned path's judge (nbg_learn_judge_stats): the last judged
+        step's p50 / p99 / RMS relative force errors of the learned and the
+        plain walk on the sampled bodies, whether that step fell back, and
+        the counts of judged and fallen-back steps."""
+        out = np.zeros(_lib.JUDGE_STATS)
+        self._check(self._lib.nbg_learn_judge_stats(
+            self._h, out.ctypes.data_as(C.POINTER(C.c_double)), out.size), "learn_judge_stats")
+        keys = ("step", "p50_learned", "p99_learned", "p50_plain", "p99_plain", "rms_learned",
+                "rms_plain", "used_plain", "samples", "judged_steps", "fallback_steps")
+        d = dict(zip(keys, out.tolist()))
+        for k in ("step", "used_plain", "samples", "judged_steps", "fallback_steps"):
+            d[k] = int(d[k])
+        d["used_plain"] = bool(d["used_plain"])
+        return d
+
+    def learn_band_rows(self) -> int:
+        """Network rows of the learned walk since the last bh_counters call
+        (read it before bh_counters, which resets it)."""
+        r = C.c_uint64(0)
+        self._check(self._lib.nbg_learn_band_rows(self._h, C.byref(r)), "learn_band_rows")
+        return r.value
 
     def tree_leaves(self) -> np.ndarray:
         n = self.problem_size() // 6

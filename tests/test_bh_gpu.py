@@ -366,3 +366,34 @@ def test_bh_mixed_refit_path(make_engine):
     e.set_step(1)  # refit: same bodies per leaf, same positions -> same forces
     f1 = _f(e, y)
     assert np.max(np.abs(f0 - f1)) == 0.0
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_bh_refit_within_step(make_engine, precision):
+    """tree_refit_within_step: a full build at the first fcompute of an engine
+    step, refits of that topology for the step's other fcomputes.  Within a
+    step the forces equal the reference rule's refit path (tree_build_rate 2,
+    an odd step refits the even step's tree) on the same positions; at the
+    next step they equal a fresh build."""
+    n = 1 << 13
+    d = NBodyData.plummer(n, seed=12)
+    y0 = d.to_state()
+    y1 = y0.copy()
+    y1[:3 * n] += 2e-3 * y0[3 * n:]  # bodies moved along their velocities
+    kw = dict(algo="bh", precision=precision, softening=1e-3, distance_to_node_radius_ratio=2.0)
+    a = make_engine(tree_refit_within_step=True, **kw)
+    assert a.init(d)
+    b = make_engine(tree_build_rate=2, **kw)
+    assert b.init(d)
+    c = make_engine(**kw)
+    assert c.init(d)
+    a.set_step(4)
+    b.set_step(4)
+    assert np.array_equal(_f(a, y0), _f(b, y0))   # both build on y0
+    b.set_step(5)
+    f_refit = _f(a, y1)                           # same step: refit to y1
+    assert np.array_equal(f_refit, _f(b, y1))     # rate 2, odd step: refit to y1
+    f_build = _f(c, y1)
+    assert not np.array_equal(f_refit, f_build)   # a rebuilt tree differs
+    a.set_step(5)
+    assert np.array_equal(_f(a, y1), f_build)     # new step: a fresh build

@@ -185,6 +185,7 @@ def test_learned_walk_vs_plain(make_engine, oracle, trained, group):
         if learned:
             e.learn_set_weights(w)
             e.tune_set("learned.group", group)
+            e.tune_set("learned.judge", 0)  # the learned walk itself, never the fallback
         f = e.create_buffer(8 * 6 * n)
         e.fcompute(0.0, e.get_y(), f)
         out = np.zeros(6 * n)
@@ -206,3 +207,128 @@ def test_learned_walk_vs_plain(make_engine, oracle, trained, group):
         assert np.quantile(learn09, 0.99) < np.quantile(plain09, 0.99)
     else:
         assert np.median(learn09) < 10 * np.median(plain09)
+
+
+# ---------------------------------------------------------------------------
+# the per-step judge and the plain fallback
+# ---------------------------------------------------------------------------
+def _splitmix64(x):
+    m = (1 << 64) - 1
+    x = (x + 0x9E3779B97F4A7C15) & m
+    x = ((x ^ (x >> 30)) * 0xBF58476D1CE4E5B9) & m
+    x = ((x ^ (x >> 27)) * 0x94D049BB133111EB) & m
+    return x ^ (x >> 31)
+
+
+def _judge_leaves(n, step, samples=4096, seed=1):
+    """The judge's sampled leaves: S = samples rounded down to a power of two
+    (at most n), leaf k (n / S) + off, off from (seed, step)."""
+    s = 1
+    while 2 * s <= min(samples, n, 4096):
+        s *= 2
+    stride = n // s
+    off = _splitmix64(((seed * 0x100000001B3) & ((1 << 64) - 1)) ^ step) % stride
+    return np.arange(s) * stride + off
+
+
+def _forces(e, n):
+    f = e.create_buffer(8 * 6 * n)
+    e.fcompute(0.0, e.get_y(), f)
+    out = np.zeros(6 * n)
+    e.read_buffer(out, f)
+    e.free_buffer(f)
+    return out
+
+
+def test_judge_trips_on_bad_weights_and_falls_back_bit_for_bit(make_engine):
+    """All-ones weights make the correction nonsense: the judge sees a learned
+    p99 above the plain theta = 0.5 walk's, and the fcompute -- and every
+    further fcompute of the same step -- equals the engine's plain theta = 0.5
+    path bit for bit (the same Hilbert tree with FP64 nodes, the same group
+    walk).  The next step is judged again."""
+    n = 1 << 15
+    d = NBodyData.plummer(n, seed=31)
+    plain = _bh_engine(make_engine, 2.0)
+    plain.tune_set("bh.fp64_nodes", 1)
+    assert plain.init(d)
+    f_plain = _forces(plain, n)
+
+    e = _bh_engine(make_engine, 1.0 / 0.9, learned=True, tight=2.0)
+    assert e.init(d)
+    e.learn_set_weights(np.ones(e.learn_param_count(), dtype=np.float32))
+    assert e.learn_judge_stats()["judged_steps"] == 0
+    f1 = _forces(e, n)
+    st = e.learn_judge_stats()
+    print(f"\nbad weights: {st}")
+    assert st["judged_steps"] == 1 and st["fallback_steps"] == 1 and st["used_plain"]
+    assert st["samples"] == 4096 and st["step"] == 0
+    assert not (st["p99_learned"] <= st["p99_plain"])  # larger, or not finite
+    assert 0.0 < st["p99_plain"] < 0.1
+    assert np.array_equal(f1, f_plain)
+    f2 = _forces(e, n)  # same step: plain again, not judged again
+    assert np.array_equal(f2, f_plain)
+    assert e.learn_judge_stats()["judged_steps"] == 1
+    e.set_step(1)
+    f3 = _forces(e, n)
+    st = e.learn_judge_stats()
+    assert st["judged_steps"] == 2 and st["fallback_steps"] == 2 and st["step"] == 1
+    assert np.array_equal(f3, f_plain)
+
+
+def test_judge_figures_and_decision(make_engine, oracle):
+    """With a correction that changes nothing (zero weights) the learned walk
+    is the warp-coherent walk at the loose ratio.  The judge's learned p50
+    and p99 equal a host recomputation on the same sampled bodies (the
+    learned walk's forces against the FP64 direct sum); its plain figures
+    equal the per-body walk at the tight ratio (the group walk forced to its
+    per-body fallback for every group) on the same bodies; and the output is
+    the learned walk's when the learned p99 is the smaller, the plain
+    path's otherwise."""
+    n = 1 << 14
+    lam_l, lam_t = 1.6, 2.0
+    d = NBodyData.plummer(n, seed=32)
+    y = d.to_state()
+    w = np.zeros(M.N_PARAMS, dtype=np.float32)
+
+    raw = _bh_engine(make_engine, lam_l, learned=True, tight=lam_t)
+    raw.tune_set("learned.judge", 0)
+    assert raw.init(d)
+    raw.learn_set_weights(w)
+    f_learned = _forces(raw, n)
+    leaves = raw.tree_leaves()
+
+    e = _bh_engine(make_engine, lam_l, learned=True, tight=lam_t)
+    assert e.init(d)
+    e.learn_set_weights(w)
+    out = _forces(e, n)
+    st = e.learn_judge_stats()
+    print(f"\nzero weights: {st}")
+
+    bodies = leaves[_judge_leaves(n, 0)]
+    a_ref = oracle.accel_rows(y, d.mass, EPS, rows=bodies)
+
+    def rel(f):
+        a = f[3 * n:].reshape(3, n).T[bodies]
+        return np.linalg.norm(a - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
+    r_l = rel(f_learned)
+    assert st["samples"] == bodies.size
+    assert np.isclose(st["p50_learned"], np.quantile(r_l, 0.5), rtol=2e-3)
+    assert np.isclose(st["p99_learned"], np.quantile(r_l, 0.99), rtol=2e-3)
+    assert np.isclose(st["rms_learned"], np.sqrt(np.mean(r_l ** 2)), rtol=2e-3)
+
+    body = _bh_engine(make_engine, lam_t)
+    body.tune_set("bh.fp64_nodes", 1)
+    body.tune_set("bh.test_cap", 1)  # every group handed to the per-body walk
+    assert body.init(d)
+    r_p = rel(_forces(body, n))
+    assert np.isclose(st["p50_plain"], np.quantile(r_p, 0.5), rtol=1e-2)
+    assert np.isclose(st["p99_plain"], np.quantile(r_p, 0.99), rtol=1e-2)
+
+    assert st["used_plain"] == (st["p99_learned"] > st["p99_plain"])
+    if st["used_plain"]:
+        plain = _bh_engine(make_engine, lam_t)
+        plain.tune_set("bh.fp64_nodes", 1)
+        assert plain.init(d)
+        assert np.array_equal(out, _forces(plain, n))
+    else:
+        assert np.array_equal(out, f_learned)

@@ -79,3 +79,65 @@ def test_noalloc_rejects_oversize(make_engine, gpulib):
     assert st == 10  # NBG_ERR_TOO_LARGE, nothing launched
     assert gpulib.nbg_status_string(st) == b"exceeds a fixed capacity"
     assert gpulib.nbg_direct_mixed_noalloc(None, None, None, 16, 1e-3, None) == 1
+
+
+_FRESH = r"""
+import ctypes as C, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from nbody_gb300 import _lib
+from nbody_gb300.data import NBodyData
+from nbody_gb300.engine import create_engine
+lib = _lib.load()
+cudart = C.CDLL("libcudart.so.13")  # the runtime the library links (already loaded)
+free, total = C.c_size_t(0), C.c_size_t(0)
+
+def free_bytes():
+    assert cudart.cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+    return free.value
+
+n, eps = 3000, 1e-3
+d = NBodyData.plummer(n, seed=5)
+e = create_engine({"engine": "gb300", "precision": "mixed", "softening": eps})
+e.tune_set("direct.symmetric", 0)
+assert e.init(d)
+y, m, f = (e.create_buffer(8 * k) for k in (6 * n, n, 6 * n))
+e.write_buffer(y, d.to_state())
+e.write_buffer(m, np.ascontiguousarray(d.mass, dtype=np.float64))
+e.synchronize()
+outs = []
+for call in range(3):
+    before = free_bytes()
+    st = lib.nbg_direct_mixed_noalloc(y.device_ptr(), m.device_ptr(), f.device_ptr(), n, eps,
+                                      lib.nbg_stream(e.handle))
+    assert st == 0, lib.nbg_status_string(st)
+    after = free_bytes()
+    if call > 0:  # the first call may load the module (the driver's own allocation)
+        assert after == before, (call, before, after)
+    out = np.zeros(6 * n)
+    e.read_buffer(out, f)
+    outs.append(out)
+g = e.create_buffer(8 * 6 * n)  # only now does an engine direct kernel run
+e.fcompute(0.0, e.get_y(), g)
+ref = np.zeros(6 * n)
+e.read_buffer(ref, g)
+for out in outs:
+    assert np.array_equal(out[:3 * n], ref[:3 * n])
+    assert np.max(np.abs(out[3 * n:] - ref[3 * n:])) <= 1e-12 * np.max(np.abs(ref[3 * n:]))
+e.close()
+print("fresh ok")
+"""
+
+
+def test_noalloc_first_call_in_fresh_process(gpulib):
+    """A process whose first direct-sum call on the GPU is the entry point
+    itself: it does the per-device set-up, gives the engine's result, and
+    later calls leave the free device memory unchanged."""
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = str(Path(__file__).resolve().parent.parent)
+    r = subprocess.run([sys.executable, "-c", _FRESH, root], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "fresh ok" in r.stdout
