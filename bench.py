@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--bh-cases", default="",
                     help="with --bh-only: comma-separated names of the suite's cases to run "
                          "(e.g. hilbert_theta_0.5); default all")
+    ap.add_argument("--bh-train-samples", type=int, default=20_000_000,
+                    help="training samples of the learned correction (the suite's learned cases)")
     ap.add_argument("--suites-out", default="bench_out/suites.json",
                     help="file for the full Barnes-Hut, ensemble and statistics results")
     return ap.parse_args()
@@ -359,17 +361,21 @@ def fp64_two_galaxies(n_bh: int):
 
 
 def bh_rkdp_run(n_bh: int, d, advises: int = 5, dt: float = 1e-3, max_recursion: int = 8,
-                refit_within_step: bool = True, max_calls: int = 3000):
+                within_step: str = "freeze", max_calls: int = 3000):
     """The 2^20-body Barnes-Hut run as the reference drives it: the rkdp solver
     (nbody/nbody_solver_rk_butcher.cpp:163-248: error threshold 1e-6 on the
     unscaled max |sum (b2 - b1) k|, the reference's default max_recursion 8
     and 8 substeps) driving the Barnes-Hut engine at theta 0.5 for `advises`
-    advise calls.  The tree is built at the first fcompute of each advise and
-    refit for every other stage and substep of it (refit_within_step), so
-    the force field the embedded error sees is continuous; rebuilding at
-    every stage instead makes the error a floor of tree noise (1e-4 - 1e-3)
-    that no step size removes.  Reported: fcompute calls, bodies/s, the
-    errors of the accepted steps, whether the recursion cap was hit."""
+    advise calls.  within_step "freeze": the tree is built at the first
+    fcompute of each advise, refit for every other stage and substep of it,
+    and every acceptance test of the advise uses the build's records, so
+    each body's force is a smooth function of the positions and the embedded
+    error measures the integration; "refit": refits without freezing
+    (acceptance tests that flip between stages leave jumps); "rebuild": a
+    tree per stage (the reference's rule at tree_build_rate 0), whose force
+    noise (1e-4 - 1e-3) no step size removes.  Reported: fcompute calls,
+    bodies/s, the errors of the accepted steps, whether the recursion cap
+    was hit."""
     from nbody_gb300.data import NBodyData
     from nbody_gb300.engine import create_engine
     from nbody_gb300.solvers import create_solver
@@ -377,7 +383,8 @@ def bh_rkdp_run(n_bh: int, d, advises: int = 5, dt: float = 1e-3, max_recursion:
     e = create_engine({"engine": "gb300", "algo": "bh", "precision": "mixed",
                        "softening": SOFTENING, "distance_to_node_radius_ratio": 2.0,
                        "tree_layout": "heap_stackless",
-                       "tree_refit_within_step": refit_within_step})
+                       "tree_refit_within_step": within_step == "refit",
+                       "tree_freeze_within_step": within_step == "freeze"})
     e.init(dd)
     s = create_solver({"solver": "rkdp", "error_threshold": 1e-6,
                        "max_recursion": max_recursion, "substep_subdivisions": 8})
@@ -411,7 +418,7 @@ def bh_rkdp_run(n_bh: int, d, advises: int = 5, dt: float = 1e-3, max_recursion:
     e.close()
     return {"advises": len(errs), "advises_asked": advises, "aborted_at_call_budget": aborted,
             "call_budget": max_calls, "dt": dt, "error_threshold": 1e-6,
-            "max_recursion": max_recursion, "refit_within_step": refit_within_step,
+            "max_recursion": max_recursion, "within_step": within_step,
             "wall_s": wall, "fcompute_calls": calls[0],
             "bodies_per_s": n_bh * calls[0] / wall, "last_errors": errs,
             "accepted_substeps": s.accepted_steps,
@@ -522,7 +529,7 @@ def train_correction(epochs: int = 8, samples: int = 20_000_000):
                "generate_s": gen_s, "train_s": train_s}
 
 
-def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
+def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None, train_samples: int = 20_000_000):
     """Plummer N = 2^20, softening 1e-3, heap_stackless, rebuilt every fcompute.
     `cases`: names of the cases to run (all when None)."""
     from nbody_gb300.data import NBodyData
@@ -539,7 +546,7 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
     learned_w = {}
 
     def learned_case():
-        w, fit = train_correction()
+        w, fit = train_correction(samples=train_samples)
         learned_w["w"] = w
         r = bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=w)
         r["training"] = fit
@@ -547,7 +554,7 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
 
     def learned_raw_case():
         if "w" not in learned_w:
-            learned_w["w"] = train_correction()[0]
+            learned_w["w"] = train_correction(samples=train_samples)[0]
         return bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=learned_w["w"],
                         judge=False)
 
@@ -597,7 +604,9 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None):
         # the same run with a tree rebuilt at every stage (the reference's
         # rule at tree_build_rate 0), recursion capped at one level
         "rkdp_theta_0.5_rebuild_every_stage": lambda: bh_rkdp_run(
-            n_bh, d, max_recursion=1, refit_within_step=False),
+            n_bh, d, max_recursion=1, within_step="rebuild"),
+        "rkdp_theta_0.5_refit_unfrozen": lambda: bh_rkdp_run(
+            n_bh, d, max_recursion=2, within_step="refit", max_calls=1000),
     }
     for name, run in suite.items():
         if cases is None or name in cases:
@@ -873,7 +882,8 @@ def run_gb300(args):
         cpu = {"value": v, "unit": "pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
                "sample": f"block engine (FP64) on {rows} of {n} rows x {n} bodies, {dt:.1f} s"}
 
-    bh = run_bh_suite(rank, args.bh_n) if (rank == 0 and not args.no_bh) else None
+    bh = run_bh_suite(rank, args.bh_n, train_samples=args.bh_train_samples) \
+        if (rank == 0 and not args.no_bh) else None
     ensemble = run_ensemble_suite(peak_flops=peak_flops) \
         if (rank == 0 and not args.no_ensemble) else None
     stats = run_stats_bench(n) if (rank == 0 and not args.no_ensemble) else None
@@ -928,7 +938,7 @@ def main():
     args = parse()
     if args.bh_only:
         cases = [c for c in args.bh_cases.split(",") if c] or None
-        print(json.dumps(run_bh_suite(0, args.bh_n, cases)), flush=True)
+        print(json.dumps(run_bh_suite(0, args.bh_n, cases, args.bh_train_samples)), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -261,8 +261,8 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       "direct.sym_g" (4 or 3: packed A-body pairs per lane of the
  *       symmetric kernel; 3 runs 5 CTAs per SM),
  *       "direct.sym_blocks" (4 or 5: CTAs per SM the symmetric kernel's
- *       register budget is set for), "direct.sym_unroll" (1, 2 or 4: unroll
- *       of its 32-step rotation loop, default 4),
+ *       register budget is set for), "direct.sym_unroll" (1, 2, 4 or 8:
+ *       unroll of its 32-step rotation loop, default 4),
  *       "direct.pairs_per_lane" (2 or 4 packed i-pairs per lane, one-sided),
  *       "direct.unroll" (2, 4 or 8: j-loop unroll),
  *       "direct.blocks_per_sm" (CTAs per SM of the persistent direct grid),
@@ -295,8 +295,11 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       "bh.refit_within_step" (0, the default: the reference's rule, a full
  *       build when tree_build_rate is 0 or step % rate == 0; 1: a full
  *       build at the first fcompute of each engine step and refits of that
- *       topology for the step's other stages, so the force field is
- *       continuous within one solver step)). */
+ *       topology for the step's other stages),
+ *       "bh.freeze_within_step" (1: as "bh.refit_within_step", and every
+ *       acceptance test of the step uses the records of the step's build,
+ *       so each body meets the same cells at every stage and its force is a
+ *       smooth function of the positions; the default group walk only)). */
 nbg_status nbg_tune_set(nbg_engine* e, const char* key, int64_t value);
 nbg_status nbg_tune_get(nbg_engine* e, const char* key, int64_t* value);
 

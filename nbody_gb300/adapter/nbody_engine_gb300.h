@@ -206,6 +206,11 @@ inline nbody_engine* nbody_create_engine_gb300(const QVariantMap& param)
 		nbg_tune_set(e->handle(), "bh.refit_within_step",
 					 param.value("tree_refit_within_step").toBool() ? 1 : 0);
 	}
+	if(param.contains("tree_freeze_within_step"))
+	{
+		nbg_tune_set(e->handle(), "bh.freeze_within_step",
+					 param.value("tree_freeze_within_step").toBool() ? 1 : 0);
+	}
 	if(param.contains("learned_judge"))
 	{
 		nbg_tune_set(e->handle(), "learned.judge", param.value("learned_judge").toBool() ? 1 : 0);

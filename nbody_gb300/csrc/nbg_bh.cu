@@ -288,7 +288,7 @@ __device__ __forceinline__ void group_pair(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f
 // SMACC: the per-body two-sum accumulators (6 BPL packed values per lane)
 // live in shared memory instead of registers; they are touched once per list
 // evaluation, and the registers they free allow more resident warps.
-template <bool CLAMP, int BPL, int ORDER, int EUNR, bool SMACC>
+template <bool CLAMP, int BPL, int ORDER, int EUNR, bool SMACC, bool FROZEN = false>
 __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, double* __restrict__ f,
                                                int n, float eps2v, const TreeState& t,
                                                int stack_cap, unsigned* err,
@@ -305,19 +305,24 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
         else return acc_reg[q];
     };
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float4 me[BPL];
+    // me: the bodies' positions for the forces; mb: for the group's box (with
+    // FROZEN, the positions of the step's build, as every acceptance test)
+    float4 me[BPL], mb[BPL];
 #pragma unroll
-    for (int b = 0; b < BPL; ++b) me[b] = __ldg(&t.node4[n + gw * 32 * BPL + b * 32 + lane]);
+    for (int b = 0; b < BPL; ++b) {
+        me[b] = __ldg(&t.node4[n + gw * 32 * BPL + b * 32 + lane]);
+        mb[b] = FROZEN ? __ldg(&t.node4_acc[n + gw * 32 * BPL + b * 32 + lane]) : me[b];
+    }
     // bounding box of the group
-    float lo[3] = {me[0].x, me[0].y, me[0].z}, hi[3] = {me[0].x, me[0].y, me[0].z};
+    float lo[3] = {mb[0].x, mb[0].y, mb[0].z}, hi[3] = {mb[0].x, mb[0].y, mb[0].z};
 #pragma unroll
     for (int b = 1; b < BPL; ++b) {
-        lo[0] = fminf(lo[0], me[b].x);
-        lo[1] = fminf(lo[1], me[b].y);
-        lo[2] = fminf(lo[2], me[b].z);
-        hi[0] = fmaxf(hi[0], me[b].x);
-        hi[1] = fmaxf(hi[1], me[b].y);
-        hi[2] = fmaxf(hi[2], me[b].z);
+        lo[0] = fminf(lo[0], mb[b].x);
+        lo[1] = fminf(lo[1], mb[b].y);
+        lo[2] = fminf(lo[2], mb[b].z);
+        hi[0] = fmaxf(hi[0], mb[b].x);
+        hi[1] = fmaxf(hi[1], mb[b].y);
+        hi[2] = fmaxf(hi[2], mb[b].z);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
@@ -453,6 +458,7 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
         // lanes past the popped entries read record 0 (unused, zeroed), and
         // leaves' second moments are zero
         const float4 nd = __ldg(&t.node4[c]);
+        const float4 nda = FROZEN ? __ldg(&t.node4_acc[c]) : nd;  // acceptance record
         const float ndm = __ldg(&t.nodem[c]);
         float4 nq0, nq1;
         if (ORDER == 2) {
@@ -465,11 +471,11 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
             if (c >= n) {
                 accept = true;
             } else {
-                const float ex = fmaxf(fabsf(nd.x - cb[0]) - hb[0], 0.f);
-                const float ey = fmaxf(fabsf(nd.y - cb[1]) - hb[1], 0.f);
-                const float ez = fmaxf(fabsf(nd.z - cb[2]) - hb[2], 0.f);
+                const float ex = fmaxf(fabsf(nda.x - cb[0]) - hb[0], 0.f);
+                const float ey = fmaxf(fabsf(nda.y - cb[1]) - hb[1], 0.f);
+                const float ez = fmaxf(fabsf(nda.z - cb[2]) - hb[2], 0.f);
                 const float dmin2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-                accept = dmin2 > nd.w;
+                accept = dmin2 > nda.w;
                 open = !accept;
             }
         }
@@ -566,7 +572,8 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
 // one from a counter, so the last groups spread over all warps instead of
 // leaving a partial wave.  A group's forces do not depend on which warp
 // computes it.
-template <bool CLAMP, int MINB, int BPL, int ORDER, int EUNR = 2, bool SMACC = false>
+template <bool CLAMP, int MINB, int BPL, int ORDER, int EUNR = 2, bool SMACC = false,
+          bool FROZEN = false>
 __global__ void __launch_bounds__(kGWThreads, MINB)
 bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n, float eps2v,
                      TreeState t, int stack_cap, unsigned* err) {
@@ -575,8 +582,8 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
     const int groups = n / (32 * BPL);
     int gw = blockIdx.x * kGWWarps + (threadIdx.x >> 5);
     while (gw < groups) {
-        group_walk_one<CLAMP, BPL, ORDER, EUNR, SMACC>(y, f, n, eps2v, t, stack_cap, err, smem_raw,
-                                                      gw);
+        group_walk_one<CLAMP, BPL, ORDER, EUNR, SMACC, FROZEN>(y, f, n, eps2v, t, stack_cap, err,
+                                                              smem_raw, gw);
         int next = 0;
         if (lane == 0) next = (int)atomicAdd(&t.fb_count[1], 1u);
         gw = gridDim.x * kGWWarps + __shfl_sync(0xffffffffu, next, 0);
@@ -699,7 +706,7 @@ bh_test_cap_kernel(int n, int stride, int samples, TreeState t, int stack_cap, u
 // tests per step.  Each lane evaluates the nodes it accepted (with the
 // quadrupole term for cells with ORDER 2) into two-sum accumulators; the
 // warp's sum is formed in FP64.
-template <bool CLAMP, int BPL, int ORDER>
+template <bool CLAMP, int BPL, int ORDER, bool FROZEN = false>
 __global__ void __launch_bounds__(kGWThreads)
 bh_body_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n, float eps2,
                     TreeState t, int stack_cap, unsigned* err) {
@@ -713,6 +720,8 @@ bh_body_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n,
         const int gw = t.fb_list[w / (32 * BPL)];
         const int leaf = n + gw * 32 * BPL + (int)(w % (32 * BPL));
         const float4 me = __ldg(&t.node4[leaf]);
+        // with FROZEN the acceptance tests use the step build's records
+        const float4 mea = FROZEN ? __ldg(&t.node4_acc[leaf]) : me;
         float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
         // (h, l) += p with the rounding error of h + p kept in l
         auto add = [](float& h, float& l, float p) {
@@ -739,7 +748,13 @@ bh_body_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n,
                 dx = nd.x - me.x;
                 dy = nd.y - me.y;
                 dz = nd.z - me.z;
-                accept = c >= n || fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > nd.w;
+                if (FROZEN) {
+                    const float4 nda = __ldg(&t.node4_acc[c]);
+                    const float ax = nda.x - mea.x, ay = nda.y - mea.y, az = nda.z - mea.z;
+                    accept = c >= n || fmaf(ax, ax, fmaf(ay, ay, az * az)) > nda.w;
+                } else {
+                    accept = c >= n || fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > nd.w;
+                }
                 open = !accept;
             }
             if (accept) {
@@ -867,18 +882,32 @@ nbg_status tree_quadrupoles(nbg_engine* e) {
 
 nbg_status bh_tree(nbg_engine* e, uint64_t step, const double* y, bool fp64_nodes, double lambda) {
     const TreeState* t = e->tree;
+    const bool freeze = e->tune_get("bh.freeze_within_step", 0) != 0;
     bool build;
     if (t == nullptr || !t->built || (fp64_nodes && t->f32))
         build = true;
-    else if (e->tune_get("bh.refit_within_step", 0) != 0)
+    else if (freeze && (t->node4_acc == nullptr || t->acc_step != t->built_step))
+        build = true;  // no acceptance records of this step's build
+    else if (freeze || e->tune_get("bh.refit_within_step", 0) != 0)
         build = step != t->built_step;
     else {
         const uint64_t rate = e->params.tree_build_rate;
         build = rate == 0 || step % rate == 0;
     }
     nbg_status s = build ? tree_build(e, y, fp64_nodes, lambda) : tree_refit(e, y, lambda);
-    if (s == NBG_OK && build) e->tree->built_step = step;
-    return s;
+    if (s != NBG_OK) return s;
+    TreeState* tt = e->tree;
+    if (build) {
+        tt->built_step = step;
+        if (freeze) {  // the acceptance records of this step
+            if (tt->node4_acc == nullptr)
+                NBG_CUDA(e, cudaMalloc(&tt->node4_acc, tt->size * sizeof(float4)));
+            NBG_CUDA(e, cudaMemcpyAsync(tt->node4_acc, tt->node4, tt->size * sizeof(float4),
+                                        cudaMemcpyDeviceToDevice, e->stream));
+            tt->acc_step = step;
+        }
+    }
+    return NBG_OK;
 }
 
 nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f) {
@@ -929,9 +958,21 @@ nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
                                        bpl == 2 ? (order == 2 ? 3 : acc_smem ? 5 : 4) : 6);
         using WalkKernel = void (*)(const double*, double*, int, float, TreeState, int, unsigned*);
         WalkKernel kern;
+        // frozen acceptance runs the default build of the walk (64-body
+        // groups, monopole cells, shared-memory accumulators, 5 CTAs per SM)
+        const bool frozen = e->tune_get("bh.freeze_within_step", 0) != 0 &&
+                            t->node4_acc != nullptr && t->acc_step == t->built_step;
+        if (frozen && !(bpl == 2 && order == 1 && acc_smem && wb >= 5 &&
+                        e->tune_get("bh.eval_unroll", 2) == 2))
+            return set_error(e, NBG_ERR_UNSUPPORTED,
+                             "bh.freeze_within_step runs the default group walk only "
+                             "(64-body groups, monopole cells)");
 #define NBG_GW(C, B) (wb >= 8 ? bh_group_walk_kernel<C, 8, B, 1> : wb >= 6 ? bh_group_walk_kernel<C, 6, B, 1> \
                       : wb >= 5 ? bh_group_walk_kernel<C, 5, B, 1> : bh_group_walk_kernel<C, 4, B, 1>)
-        if (order == 2 && bpl == 2 && wb <= 3)
+        if (frozen)
+            kern = clamp ? bh_group_walk_kernel<true, 5, 2, 1, 2, true, true>
+                         : bh_group_walk_kernel<false, 5, 2, 1, 2, true, true>;
+        else if (order == 2 && bpl == 2 && wb <= 3)
             kern = clamp ? bh_group_walk_kernel<true, 3, 2, 2> : bh_group_walk_kernel<false, 3, 2, 2>;
         else if (order == 2)
             kern = bpl == 2 ? (clamp ? bh_group_walk_kernel<true, 4, 2, 2> : bh_group_walk_kernel<false, 4, 2, 2>)
@@ -984,7 +1025,11 @@ nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
             auto capk = bpl == 2 ? bh_test_cap_kernel<2> : bh_test_cap_kernel<1>;
             NBG_CUDA(e, cudaFuncSetAttribute(capk, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)csmem));
-            capk<<<1, kCapSamples * 32, csmem, e->stream>>>(n, warps / samples, samples, *t,
+            // the cap counts acceptance tests: against the step build's
+            // records when those decide acceptance
+            TreeState tc = *t;
+            if (frozen) tc.node4 = t->node4_acc;
+            capk<<<1, kCapSamples * 32, csmem, e->stream>>>(n, warps / samples, samples, tc,
                                                             stack_cap, ratio);
             NBG_LAUNCHED(e, "bh_test_cap_kernel");
         }
@@ -1000,7 +1045,9 @@ nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
         }
         kern<<<blocks, kGWThreads, smem, e->stream>>>(y, f, n, eps2, *t, stack_cap, e->d_err);
         NBG_LAUNCHED(e, "bh_group_walk_kernel");
-        auto fb = order == 2
+        auto fb = frozen
+            ? (clamp ? bh_body_walk_kernel<true, 2, 1, true> : bh_body_walk_kernel<false, 2, 1, true>)
+            : order == 2
             ? (clamp ? (bpl == 2 ? bh_body_walk_kernel<true, 2, 2> : bh_body_walk_kernel<true, 1, 2>)
                      : (bpl == 2 ? bh_body_walk_kernel<false, 2, 2> : bh_body_walk_kernel<false, 1, 2>))
             : (clamp ? (bpl == 2 ? bh_body_walk_kernel<true, 2, 1> : bh_body_walk_kernel<true, 1, 1>)
@@ -1012,6 +1059,9 @@ nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
         NBG_LAUNCHED(e, "bh_body_walk_kernel");
         return NBG_OK;
     }
+    if (e->tune_get("bh.freeze_within_step", 0) != 0)
+        return set_error(e, NBG_ERR_UNSUPPORTED,
+                         "bh.freeze_within_step runs the default group walk only");
     // warps past n still walk (their lanes mirror the last body) so that
     // every warp is full; n is a power of two, so only n < 32 has such lanes
     const int threads = ((n + 31) / 32) * 32;

@@ -642,7 +642,7 @@ nbg_status direct_sym_launch(nbg_engine* e, const double* y, double* f) {
     const bool clamp = !(e->params.softening > 0.0);
     // "direct.sym_blocks": CTAs per SM the register budget is set for
     // (4: 128 registers, 5: 102)
-    // "direct.sym_unroll": unroll of the 32-step rotation loop (1, 2 or 4)
+    // "direct.sym_unroll": unroll of the 32-step rotation loop (1, 2, 4 or 8)
     const bool b5 = e->tune_get("direct.sym_blocks", 4) >= 5;
     const int64_t ru = e->tune_get("direct.sym_unroll", 4);
     using SymKernel = void (*)(SymArgs);
@@ -651,6 +651,8 @@ nbg_status direct_sym_launch(nbg_engine* e, const double* y, double* f) {
         kern = clamp ? direct_sym_kernel<true, 5, 4, 3> : direct_sym_kernel<false, 5, 4, 3>;
     else if (b5)
         kern = clamp ? direct_sym_kernel<true, 5, 2> : direct_sym_kernel<false, 5, 2>;
+    else if (ru >= 8)
+        kern = clamp ? direct_sym_kernel<true, 4, 8> : direct_sym_kernel<false, 4, 8>;
     else if (ru >= 4)
         kern = clamp ? direct_sym_kernel<true, 4, 4> : direct_sym_kernel<false, 4, 4>;
     else if (ru <= 1)

@@ -47,6 +47,13 @@ struct TreeState {
     bool f32 = false;
     float4* box4 = nullptr;   // [2][size]
 
+    // frozen acceptance ("bh.freeze_within_step"): the FP32 records of the
+    // step's full build, which the walks test acceptance (and form group
+    // boxes) against while the refit records of the step's later stages
+    // give the forces; null when not in use
+    float4* node4_acc = nullptr;  // [size]
+    uint64_t acc_step = 0;        // built_step of the records in node4_acc
+
     // learned-correction node features (quadrupole, spread), see nbg_learned.cu
     float4* feat = nullptr;   // [3][size] or null
 
@@ -88,8 +95,12 @@ nbg_status tree_refit(nbg_engine* e, const double* y, double lambda);
 // builds when tree_build_rate is 0 or step % rate == 0 and refits otherwise.
 // With "bh.refit_within_step" = 1 the engine builds only at the first
 // fcompute of each engine step (the step number changes) and refits for the
-// other stages of that step, so that the force field stays continuous
-// within a solver step (the solver advances the step once per advise).  A
+// other stages of that step (the solver advances the step once per advise).
+// "bh.freeze_within_step" = 1 does the same and also keeps the step build's
+// records for the acceptance tests, so every body interacts with the same
+// cells at every stage of the step and its force is a smooth function of
+// the positions (the refit moves the cells' mass centres); without it an
+// acceptance test that flips between stages puts a jump in the force.  A
 // caller that needs the FP64 node arrays (fp64_nodes) gets a build when the
 // last one formed only the FP32 records.
 nbg_status bh_tree(nbg_engine* e, uint64_t step, const double* y, bool fp64_nodes, double lambda);

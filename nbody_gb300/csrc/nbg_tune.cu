@@ -55,7 +55,7 @@ std::vector<Candidate> direct_candidates() {
     for (int bps : {0, 3, 2})
         c.push_back({{"direct.symmetric", 1}, {"direct.sym_blocks", 4}, {"direct.blocks_per_sm", bps}});
     c.push_back({{"direct.symmetric", 1}, {"direct.sym_blocks", 5}, {"direct.blocks_per_sm", 0}});
-    for (int ru : {1, 2})
+    for (int ru : {1, 2, 8})
         c.push_back({{"direct.symmetric", 1}, {"direct.sym_blocks", 4}, {"direct.sym_unroll", ru},
                      {"direct.blocks_per_sm", 0}});
     c.push_back({{"direct.symmetric", 1}, {"direct.sym_g", 3}, {"direct.blocks_per_sm", 0}});

@@ -117,6 +117,8 @@ def create_engine(param: dict) -> Optional["NbodyEngineGB300"]:
     try:
         if "tree_refit_within_step" in param:
             tune["bh.refit_within_step"] = int(bool(param["tree_refit_within_step"]))
+        if "tree_freeze_within_step" in param:
+            tune["bh.freeze_within_step"] = int(bool(param["tree_freeze_within_step"]))
         if "learned_judge" in param:
             tune["learned.judge"] = int(bool(param["learned_judge"]))
         if "learned_judge_samples" in param:

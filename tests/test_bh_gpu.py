@@ -397,3 +397,38 @@ def test_bh_refit_within_step(make_engine, precision):
     assert not np.array_equal(f_refit, f_build)   # a rebuilt tree differs
     a.set_step(5)
     assert np.array_equal(_f(a, y1), f_build)     # new step: a fresh build
+
+
+def test_bh_freeze_within_step(make_engine):
+    """tree_freeze_within_step: at the step's build the forces equal the
+    plain walk's bit for bit; at a later stage of the same step, with the
+    bodies moved, every body meets exactly the cells of the build (the same
+    interaction count), while an unfrozen refit changes the accepted sets.
+    The next step builds afresh."""
+    n = 1 << 15
+    d = NBodyData.plummer(n, seed=13)
+    y0 = d.to_state()
+    y1 = y0.copy()
+    y1[:3 * n] += 5e-3 * y0[3 * n:]
+    kw = dict(algo="bh", precision="mixed", softening=1e-3, distance_to_node_radius_ratio=2.0)
+    fz = make_engine(tree_freeze_within_step=True, **kw)
+    rf = make_engine(tree_refit_within_step=True, **kw)
+    pl = make_engine(**kw)
+    for e in (fz, rf, pl):
+        assert e.init(d)
+        e.set_step(7)
+    f0 = _f(fz, y0)
+    _, i_build = fz.bh_counters()
+    assert np.array_equal(f0, _f(pl, y0))
+    _f(rf, y0)
+    rf.bh_counters()
+    f1 = _f(fz, y1)                  # same step: refit, acceptance frozen
+    _, i_frozen = fz.bh_counters()
+    _f(rf, y1)
+    _, i_refit = rf.bh_counters()
+    assert i_frozen == i_build
+    assert i_refit != i_build
+    assert np.all(np.isfinite(f1)) and not np.array_equal(f1, f0)
+    fz.set_step(8)
+    pl.set_step(8)
+    assert np.array_equal(_f(fz, y1), _f(pl, y1))  # new step: a fresh build
