@@ -266,6 +266,9 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       "direct.pairs_per_lane" (2 or 4 packed i-pairs per lane, one-sided),
  *       "direct.unroll" (2, 4 or 8: j-loop unroll),
  *       "direct.blocks_per_sm" (CTAs per SM of the persistent direct grid),
+ *       "direct.uniform_mass" (1, the default: when every body has the same
+ *       mass the symmetric kernel weights pairs by r^-3 alone and scales the
+ *       sums by the mass once, in FP64; 0: the general kernel),
  *       "bh.walk" (1: group walk with interaction lists, 0: warp-coherent
  *       stackless walk) for the mixed-precision Barnes-Hut path,
  *       "bh.group" (64 or 32 bodies per warp in the group walk),

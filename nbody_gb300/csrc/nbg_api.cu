@@ -347,6 +347,11 @@ nbg_status nbg_init(nbg_engine* e, size_t count, const double* vertices,
         }
     std::vector<float> mf(count);
     for (size_t i = 0; i < count; ++i) mf[i] = (float)mass[i];
+    // equal masses (a common initial condition) let the mixed direct kernel
+    // scale the pair sums by the mass once instead of weighting every pair
+    e->uniform_mass = true;
+    for (size_t i = 1; i < count && e->uniform_mass; ++i) e->uniform_mass = mass[i] == mass[0];
+    e->mass_value = mass[0];
     NBG_CUDA(e, cudaMemcpy(y->dptr, h.data(), 6 * count * sizeof(double),
                            cudaMemcpyHostToDevice));
     NBG_CUDA(e, cudaMemcpy(e->d_mass, mass, count * sizeof(double), cudaMemcpyHostToDevice));

@@ -50,6 +50,8 @@ struct nbg_engine {
     nbg_buffer* y = nullptr;     // state [6N] doubles
     double* d_mass = nullptr;    // [N]
     float* d_massf = nullptr;    // [N] (mixed paths)
+    bool uniform_mass = false;   // every body has the mass mass_value
+    double mass_value = 0.0;
 
     // direct-sum scratch: packed FP32 bodies (x, y, z, m), padded to tiles
     float4* d_xyzm = nullptr;

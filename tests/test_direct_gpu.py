@@ -82,14 +82,17 @@ def test_config1_fp64_rk4_100_steps(make_engine, oracle):
     assert np.allclose(dg, dr, rtol=1e-6, atol=1e-12)
 
 
-@pytest.mark.parametrize("sym", [0, 1])
+@pytest.mark.parametrize("sym", [0, 1, 2])
 def test_mixed_plummer_force_error(make_engine, oracle, sym):
-    """Both mixed kernels (0: one-sided, 1: each unordered pair once) on
-    every row against the FP64 direct sum."""
+    """The mixed kernels (0: one-sided, 1: each unordered pair once, with the
+    uniform-mass kernel the equal masses select; 2: the same with the
+    general, mass-weighted kernel) on every row against the FP64 direct sum."""
     n = 16384
     d = NBodyData.plummer(n, seed=7)
     e = make_engine(precision="mixed", softening=1e-3)
-    e.tune_set("direct.symmetric", sym)
+    e.tune_set("direct.symmetric", min(sym, 1))
+    if sym == 2:
+        e.tune_set("direct.uniform_mass", 0)
     assert e.init(d)
     y = d.to_state()
     f = _f_gpu(e, y)
@@ -149,3 +152,33 @@ def test_full_size_sampled_and_momentum(make_engine, oracle, sym):
     net = np.abs((d.mass[:, None] * a).sum(axis=0))
     scale = (d.mass[:, None] * np.abs(a)).sum(axis=0)
     assert np.all(net <= 1e-5 * scale)
+
+
+def test_uniform_mass_kernel_equals_general(make_engine, oracle):
+    """Equal masses: the kernel that scales the pair sums by the mass once
+    agrees with the mass-weighted kernel (both FP32 pairs, two-sum tiles) to
+    FP32 rounding, and unequal masses never select it."""
+    n = 8192
+    d = NBodyData.plummer(n, seed=21)
+    assert np.all(d.mass == d.mass[0])
+    out = []
+    for uni in (1, 0):
+        e = make_engine(precision="mixed", softening=1e-3)
+        e.tune_set("direct.uniform_mass", uni)
+        assert e.init(d)
+        out.append(_f_gpu(e, d.to_state()))
+    a_u, a_g = (o[3 * n:].reshape(3, n).T for o in out)
+    rel = _rel_err(a_u, a_g)
+    assert np.sqrt(np.mean(rel ** 2)) < 5e-7 and rel.max() < 1e-4
+    # a single differing mass switches the specialisation off: same result
+    # as the general kernel, bit for bit except for atomic ordering
+    d2 = NBodyData.plummer(n, seed=21)
+    d2.mass = d2.mass.copy()
+    d2.mass[17] *= 1.5
+    e1 = make_engine(precision="mixed", softening=1e-3)
+    assert e1.init(d2)
+    e2 = make_engine(precision="mixed", softening=1e-3)
+    e2.tune_set("direct.uniform_mass", 0)
+    assert e2.init(d2)
+    f1, f2 = _f_gpu(e1, d2.to_state()), _f_gpu(e2, d2.to_state())
+    assert np.max(np.abs(f1 - f2)) <= 1e-12 * np.max(np.abs(f2))
