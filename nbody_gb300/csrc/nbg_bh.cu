@@ -969,9 +969,12 @@ nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
                              "(64-body groups, monopole cells)");
 #define NBG_GW(C, B) (wb >= 8 ? bh_group_walk_kernel<C, 8, B, 1> : wb >= 6 ? bh_group_walk_kernel<C, 6, B, 1> \
                       : wb >= 5 ? bh_group_walk_kernel<C, 5, B, 1> : bh_group_walk_kernel<C, 4, B, 1>)
-        if (frozen)
+        if (frozen) {
+            // the default build keeps its accumulators in shared memory
+            smem += (size_t)kGWThreads * 6 * 2 * sizeof(f2_t);
             kern = clamp ? bh_group_walk_kernel<true, 5, 2, 1, 2, true, true>
                          : bh_group_walk_kernel<false, 5, 2, 1, 2, true, true>;
+        }
         else if (order == 2 && bpl == 2 && wb <= 3)
             kern = clamp ? bh_group_walk_kernel<true, 3, 2, 2> : bh_group_walk_kernel<false, 3, 2, 2>;
         else if (order == 2)

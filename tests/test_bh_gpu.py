@@ -381,12 +381,13 @@ def test_bh_refit_within_step(make_engine, precision):
     y1 = y0.copy()
     y1[:3 * n] += 2e-3 * y0[3 * n:]  # bodies moved along their velocities
     kw = dict(algo="bh", precision=precision, softening=1e-3, distance_to_node_radius_ratio=2.0)
+    # each engine its own data: the data object holds the step counter
     a = make_engine(tree_refit_within_step=True, **kw)
-    assert a.init(d)
+    assert a.init(NBodyData.plummer(n, seed=12))
     b = make_engine(tree_build_rate=2, **kw)
-    assert b.init(d)
+    assert b.init(NBodyData.plummer(n, seed=12))
     c = make_engine(**kw)
-    assert c.init(d)
+    assert c.init(NBodyData.plummer(n, seed=12))
     a.set_step(4)
     b.set_step(4)
     assert np.array_equal(_f(a, y0), _f(b, y0))   # both build on y0
@@ -414,8 +415,8 @@ def test_bh_freeze_within_step(make_engine):
     fz = make_engine(tree_freeze_within_step=True, **kw)
     rf = make_engine(tree_refit_within_step=True, **kw)
     pl = make_engine(**kw)
-    for e in (fz, rf, pl):
-        assert e.init(d)
+    for e in (fz, rf, pl):  # each engine its own data (it holds the step)
+        assert e.init(NBodyData.plummer(n, seed=13))
         e.set_step(7)
     f0 = _f(fz, y0)
     _, i_build = fz.bh_counters()
