@@ -240,8 +240,10 @@ def run_reference(args):
                        "has none) instead of softening 1e-3",
                        "Euler steps (1 fcompute) instead of rk4 steps (4 fcomputes); the "
                        "metric counts pairs either way"],
-                   "cpu": "block engine restated in oracle/ (OpenMP over all host threads); "
-                          "the reference's own build needs Qt, absent on this host"},
+                   "cpu": "the reference's block engine restated in oracle/ (OpenMP over all "
+                          "host threads); the reference's sources are not on this host, and "
+                          "where they are the restatement equals the reference's own build bit "
+                          "for bit (tests/test_ref_pin.py)"},
         "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
                          "sample": f"whole steps: {args.steps} timed Euler steps of the full "
                                    f"{n}-body workload after {args.warmup} warm-up steps"},

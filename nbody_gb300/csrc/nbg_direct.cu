@@ -369,7 +369,11 @@ __global__ void pack_sym_kernel(const double* __restrict__ y, const double* __re
                                 int n_pad) {
     int stride = gridDim.x * blockDim.x;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += stride) {
-        float4 xy = make_float4(0.f, 0.f, 0.f, 0.f), zm = xy;
+        // padding bodies: zero mass, and parked at 1e18 on every axis, where
+        // r^-3 underflows to exactly 0 in FP32, so that they add nothing in
+        // the uniform-mass kernel, which does not weight pairs by mass either
+        float4 xy = make_float4(1e18f, 1e18f, 1e18f, 1e18f);
+        float4 zm = make_float4(1e18f, 1e18f, 0.f, 0.f);
         if (i < n) {
             const float x = (float)y[i], yy = (float)y[n + i], z = (float)y[2 * n + i];
             const float m = (float)mass[i];

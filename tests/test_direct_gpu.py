@@ -154,22 +154,32 @@ def test_full_size_sampled_and_momentum(make_engine, oracle, sym):
     assert np.all(net <= 1e-5 * scale)
 
 
-def test_uniform_mass_kernel_equals_general(make_engine, oracle):
+@pytest.mark.parametrize("n,g", [(8192, 4), (5000, 4), (16384, 3), (1000, 3), (1, 4)])
+def test_uniform_mass_kernel_equals_general(make_engine, oracle, n, g):
     """Equal masses: the kernel that scales the pair sums by the mass once
     agrees with the mass-weighted kernel (both FP32 pairs, two-sum tiles) to
-    FP32 rounding, and unequal masses never select it."""
-    n = 8192
+    FP32 rounding and with the FP64 direct sum, also when the last range is
+    padded (n not a multiple of the 256 g-body range: the padding must add
+    nothing), and unequal masses never select it."""
     d = NBodyData.plummer(n, seed=21)
     assert np.all(d.mass == d.mass[0])
     out = []
     for uni in (1, 0):
         e = make_engine(precision="mixed", softening=1e-3)
         e.tune_set("direct.uniform_mass", uni)
+        e.tune_set("direct.sym_g", g)
         assert e.init(d)
         out.append(_f_gpu(e, d.to_state()))
+    if n == 1:
+        assert np.all(out[0][3:] == 0.0) and np.all(out[1][3:] == 0.0)
+        return
     a_u, a_g = (o[3 * n:].reshape(3, n).T for o in out)
     rel = _rel_err(a_u, a_g)
     assert np.sqrt(np.mean(rel ** 2)) < 5e-7 and rel.max() < 1e-4
+    a_ref = oracle.accel_rows(d.to_state(), d.mass, 1e-3)
+    assert np.sqrt(np.mean(_rel_err(a_u, a_ref) ** 2)) <= 1e-6
+    if n != 8192 or g != 4:
+        return
     # a single differing mass switches the specialisation off: same result
     # as the general kernel, bit for bit except for atomic ordering
     d2 = NBodyData.plummer(n, seed=21)
