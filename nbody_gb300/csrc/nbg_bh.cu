@@ -283,6 +283,33 @@ __device__ __forceinline__ void group_pair(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f
     az = f2_fma(dz, s3, az);
 }
 
+// The pair term with positions split as FP32 hi + lo (frozen acceptance):
+// d = (x_j - x_i) + (lo_j - lo_i), so a close pair's difference keeps the
+// bits the FP32 rounding of its absolute positions drops.
+template <bool CLAMP>
+__device__ __forceinline__ void group_pair_lo(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f2_t lxj,
+                                              f2_t lyj, f2_t lzj, f2_t xi, f2_t yi, f2_t zi,
+                                              f2_t lxi, f2_t lyi, f2_t lzi, f2_t eps2, f2_t& ax,
+                                              f2_t& ay, f2_t& az) {
+    const f2_t dx = f2_add(f2_sub(xj, xi), f2_sub(lxj, lxi));
+    const f2_t dy = f2_add(f2_sub(yj, yi), f2_sub(lyj, lyi));
+    const f2_t dz = f2_add(f2_sub(zj, zi), f2_sub(lzj, lzi));
+    f2_t r2 = f2_fma(dz, dz, eps2);
+    r2 = f2_fma(dy, dy, r2);
+    r2 = f2_fma(dx, dx, r2);
+    float r2a, r2b;
+    f2_unpack(r2, r2a, r2b);
+    if (CLAMP) {
+        r2a = fmaxf(r2a, 1e-8f);
+        r2b = fmaxf(r2b, 1e-8f);
+    }
+    const f2_t inv = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
+    const f2_t s3 = f2_mul(f2_mul(mj, inv), f2_mul(inv, inv));
+    ax = f2_fma(dx, s3, ax);
+    ay = f2_fma(dy, s3, ay);
+    az = f2_fma(dz, s3, az);
+}
+
 // BPL bodies per lane: a group of 32 BPL consecutive leaves per warp (lane l
 // holds leaves l, l + 32, ...); every list entry is evaluated for all of them.
 // SMACC: the per-body two-sum accumulators (6 BPL packed values per lane)
@@ -349,11 +376,25 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
     const f2_t eps2 = f2_pack(eps2v, eps2v);
     const f2_t zero = f2_pack(0.f, 0.f);
     f2_t xi[BPL], yi[BPL], zi[BPL];
+    // FROZEN: the bodies' FP32 residuals, and per-warp residual lists beside
+    // the interaction list (after the shared-memory accumulators; zero for
+    // cells)
+    f2_t xil[FROZEN ? BPL : 1], yil[FROZEN ? BPL : 1], zil[FROZEN ? BPL : 1];
+    float* llx = reinterpret_cast<float*>(reinterpret_cast<f2_t*>(stacks + kGWWarps * stack_cap) +
+                                          (SMACC ? kGWThreads * 6 * BPL : 0)) + warp * kGWList;
+    float* lly = llx + kGWWarps * kGWList;
+    float* llz = lly + kGWWarps * kGWList;
 #pragma unroll
     for (int b = 0; b < BPL; ++b) {
         xi[b] = f2_pack(me[b].x, me[b].x);
         yi[b] = f2_pack(me[b].y, me[b].y);
         zi[b] = f2_pack(me[b].z, me[b].z);
+        if constexpr (FROZEN) {
+            const float4 lo = __ldg(&t.leaf_lo[gw * 32 * BPL + b * 32 + lane]);
+            xil[b] = f2_pack(lo.x, lo.x);
+            yil[b] = f2_pack(lo.y, lo.y);
+            zil[b] = f2_pack(lo.z, lo.z);
+        }
 #pragma unroll
         for (int q = 0; q < 6; ++q) slot(6 * b + q) = zero;
     }
@@ -373,12 +414,42 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
             ly[lc + lane] = 0.f;
             lz[lc + lane] = 0.f;
             lm[lc + lane] = 0.f;
+            if constexpr (FROZEN) {
+                llx[lc + lane] = 0.f;
+                lly[lc + lane] = 0.f;
+                llz[lc + lane] = 0.f;
+            }
         }
         __syncwarp();
         f2_t ax[BPL], ay[BPL], az[BPL], bx[BPL], by[BPL], bz[BPL];
 #pragma unroll
         for (int b = 0; b < BPL; ++b) ax[b] = ay[b] = az[b] = bx[b] = by[b] = bz[b] = zero;
         const int quads = (lc + 3) >> 2;
+        if constexpr (FROZEN) {
+            const uint32_t lx_addr = smem_addr(llx), ly_addr = smem_addr(lly);
+            const uint32_t lz_addr = smem_addr(llz);
+#pragma unroll 1
+            for (int r = 0; r < quads; ++r) {
+                const float4 X = lds128(ax_addr + 16u * r);
+                const float4 Y = lds128(ay_addr + 16u * r);
+                const float4 Z = lds128(az_addr + 16u * r);
+                const float4 M = lds128(am_addr + 16u * r);
+                const float4 LX = lds128(lx_addr + 16u * r);
+                const float4 LY = lds128(ly_addr + 16u * r);
+                const float4 LZ = lds128(lz_addr + 16u * r);
+#pragma unroll
+                for (int b = 0; b < BPL; ++b) {
+                    group_pair_lo<CLAMP>(f2_pack(X.x, X.y), f2_pack(Y.x, Y.y), f2_pack(Z.x, Z.y),
+                                         f2_pack(M.x, M.y), f2_pack(LX.x, LX.y),
+                                         f2_pack(LY.x, LY.y), f2_pack(LZ.x, LZ.y), xi[b], yi[b],
+                                         zi[b], xil[b], yil[b], zil[b], eps2, ax[b], ay[b], az[b]);
+                    group_pair_lo<CLAMP>(f2_pack(X.z, X.w), f2_pack(Y.z, Y.w), f2_pack(Z.z, Z.w),
+                                         f2_pack(M.z, M.w), f2_pack(LX.z, LX.w),
+                                         f2_pack(LY.z, LY.w), f2_pack(LZ.z, LZ.w), xi[b], yi[b],
+                                         zi[b], xil[b], yil[b], zil[b], eps2, bx[b], by[b], bz[b]);
+                }
+            }
+        } else {
 #pragma unroll EUNR
         for (int r = 0; r < quads; ++r) {
             const float4 X = lds128(ax_addr + 16u * r);
@@ -394,6 +465,7 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
                                   f2_pack(M.z, M.w), xi[b], yi[b], zi[b], eps2, bx[b], by[b],
                                   bz[b]);
             }
+        }
         }
 #pragma unroll
         for (int b = 0; b < BPL; ++b) {
@@ -498,6 +570,12 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
             ly[q] = nd.y;
             lz[q] = nd.z;
             lm[q] = ndm;
+            if constexpr (FROZEN) {  // leaves carry their residuals, cells none
+                const float4 lo = c >= n ? __ldg(&t.leaf_lo[c - n]) : make_float4(0.f, 0.f, 0.f, 0.f);
+                llx[q] = lo.x;
+                lly[q] = lo.y;
+                llz[q] = lo.z;
+            }
         }
         lc += __popc(am);
         if (ORDER == 2) {
@@ -720,8 +798,10 @@ bh_body_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n,
         const int gw = t.fb_list[w / (32 * BPL)];
         const int leaf = n + gw * 32 * BPL + (int)(w % (32 * BPL));
         const float4 me = __ldg(&t.node4[leaf]);
-        // with FROZEN the acceptance tests use the step build's records
+        // with FROZEN the acceptance tests use the step build's records, and
+        // pair differences add the leaves' FP32 residuals
         const float4 mea = FROZEN ? __ldg(&t.node4_acc[leaf]) : me;
+        const float4 mel = FROZEN ? __ldg(&t.leaf_lo[leaf - n]) : make_float4(0.f, 0.f, 0.f, 0.f);
         float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
         // (h, l) += p with the rounding error of h + p kept in l
         auto add = [](float& h, float& l, float p) {
@@ -749,6 +829,11 @@ bh_body_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n,
                 dy = nd.y - me.y;
                 dz = nd.z - me.z;
                 if (FROZEN) {
+                    const float4 lo =
+                        c >= n ? __ldg(&t.leaf_lo[c - n]) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    dx += lo.x - mel.x;
+                    dy += lo.y - mel.y;
+                    dz += lo.z - mel.z;
                     const float4 nda = __ldg(&t.node4_acc[c]);
                     const float ax = nda.x - mea.x, ay = nda.y - mea.y, az = nda.z - mea.z;
                     accept = c >= n || fmaf(ax, ax, fmaf(ay, ay, az * az)) > nda.w;
@@ -880,6 +965,18 @@ nbg_status tree_quadrupoles(nbg_engine* e) {
 
 }  // namespace
 
+namespace {
+// Residual of each leaf's FP32 position (frozen acceptance): lo = y - hi.
+__global__ void leaf_lo_kernel(const double* __restrict__ y, int n, TreeState t) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const int b = t.body_n[n + p];
+        const float4 hi = t.node4[n + p];
+        t.leaf_lo[p] = make_float4((float)(y[b] - (double)hi.x), (float)(y[n + b] - (double)hi.y),
+                                   (float)(y[2 * n + b] - (double)hi.z), 0.f);
+    }
+}
+}  // namespace
+
 nbg_status bh_tree(nbg_engine* e, uint64_t step, const double* y, bool fp64_nodes, double lambda) {
     const TreeState* t = e->tree;
     const bool freeze = e->tune_get("bh.freeze_within_step", 0) != 0;
@@ -906,6 +1003,14 @@ nbg_status bh_tree(nbg_engine* e, uint64_t step, const double* y, bool fp64_node
                                         cudaMemcpyDeviceToDevice, e->stream));
             tt->acc_step = step;
         }
+    }
+    if (freeze) {  // the leaves' residuals, at every build and refit
+        if (tt->leaf_lo == nullptr)
+            NBG_CUDA(e, cudaMalloc(&tt->leaf_lo, tt->n * sizeof(float4)));
+        const int n = (int)tt->n;
+        leaf_lo_kernel<<<grid_for(n, 256, (unsigned)e->sm_count * 8u), 256, 0, e->stream>>>(
+            y, n, *tt);
+        NBG_LAUNCHED(e, "leaf_lo_kernel");
     }
     return NBG_OK;
 }
@@ -958,22 +1063,25 @@ nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
                                        bpl == 2 ? (order == 2 ? 3 : acc_smem ? 5 : 4) : 6);
         using WalkKernel = void (*)(const double*, double*, int, float, TreeState, int, unsigned*);
         WalkKernel kern;
-        // frozen acceptance runs the default build of the walk (64-body
-        // groups, monopole cells, shared-memory accumulators, 5 CTAs per SM)
+        // frozen acceptance runs its own build of the default walk (64-body
+        // groups, monopole cells, shared-memory accumulators, residual
+        // lists; a 4-CTA register budget)
         const bool frozen = e->tune_get("bh.freeze_within_step", 0) != 0 &&
-                            t->node4_acc != nullptr && t->acc_step == t->built_step;
-        if (frozen && !(bpl == 2 && order == 1 && acc_smem && wb >= 5 &&
-                        e->tune_get("bh.eval_unroll", 2) == 2))
+                            t->node4_acc != nullptr && t->acc_step == t->built_step &&
+                            t->leaf_lo != nullptr;
+        if (frozen && !(bpl == 2 && order == 1 && acc_smem))
             return set_error(e, NBG_ERR_UNSUPPORTED,
                              "bh.freeze_within_step runs the default group walk only "
                              "(64-body groups, monopole cells)");
 #define NBG_GW(C, B) (wb >= 8 ? bh_group_walk_kernel<C, 8, B, 1> : wb >= 6 ? bh_group_walk_kernel<C, 6, B, 1> \
                       : wb >= 5 ? bh_group_walk_kernel<C, 5, B, 1> : bh_group_walk_kernel<C, 4, B, 1>)
         if (frozen) {
-            // the default build keeps its accumulators in shared memory
-            smem += (size_t)kGWThreads * 6 * 2 * sizeof(f2_t);
-            kern = clamp ? bh_group_walk_kernel<true, 5, 2, 1, 2, true, true>
-                         : bh_group_walk_kernel<false, 5, 2, 1, 2, true, true>;
+            // the default build keeps its accumulators in shared memory, and
+            // the frozen walk three residual lists per warp after them
+            smem += (size_t)kGWThreads * 6 * 2 * sizeof(f2_t) +
+                    (size_t)3 * kGWWarps * kGWList * sizeof(float);
+            kern = clamp ? bh_group_walk_kernel<true, 4, 2, 1, 2, true, true>
+                         : bh_group_walk_kernel<false, 4, 2, 1, 2, true, true>;
         }
         else if (order == 2 && bpl == 2 && wb <= 3)
             kern = clamp ? bh_group_walk_kernel<true, 3, 2, 2> : bh_group_walk_kernel<false, 3, 2, 2>;

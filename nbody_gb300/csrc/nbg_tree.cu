@@ -639,7 +639,8 @@ void tree_destroy(nbg_engine* e) {
                     t->lists[2], t->spare[0], t->spare[1], t->flag, t->tile_count, t->hist, t->totals, t->box,
                     t->fb_list, t->fb_count, t->cap_state,
                     t->com, t->mass, t->bmin, t->bmax, t->crit2, t->body_n, t->node4,
-                    t->nodem, t->box4, t->feat, t->quad, t->counters, t->node4_acc};
+                    t->nodem, t->box4, t->feat, t->quad, t->counters, t->node4_acc,
+                    t->leaf_lo};
     for (void* p : ptrs) cudaFree(p);
     delete t;
     e->tree = nullptr;

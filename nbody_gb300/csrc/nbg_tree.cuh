@@ -53,6 +53,12 @@ struct TreeState {
     // give the forces; null when not in use
     float4* node4_acc = nullptr;  // [size]
     uint64_t acc_step = 0;        // built_step of the records in node4_acc
+    // with frozen acceptance, each leaf's FP32 rounding residual (x - hi,
+    // y - hi, z - hi, 0) of the position in node4, so that the walks form
+    // pair differences as (x_j - x_i) + (lo_j - lo_i): the FP32 rounding of
+    // absolute positions would otherwise change a close pair's force in
+    // steps as the bodies move within a step
+    float4* leaf_lo = nullptr;    // [n]
 
     // learned-correction node features (quadrupole, spread), see nbg_learned.cu
     float4* feat = nullptr;   // [3][size] or null
