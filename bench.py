@@ -550,14 +550,15 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None, train_samples: int 
     def learned_case():
         w, fit = train_correction(samples=train_samples)
         learned_w["w"] = w
-        r = bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=w)
+        # the learned walk is its own kernel; the fallback is the default walk
+        r = bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, weights=w)
         r["training"] = fit
         return r
 
     def learned_raw_case():
         if "w" not in learned_w:
             learned_w["w"] = train_correction(samples=train_samples)[0]
-        return bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, walk=0, weights=learned_w["w"],
+        return bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, weights=learned_w["w"],
                         judge=False)
 
     suite = {
