@@ -382,7 +382,10 @@ nbg_status nbg_ensemble_fcompute(nbg_ensemble* s, double* f);
 nbg_status nbg_ensemble_statistics(nbg_ensemble* s, double* out);
 /* Tuning keys "ensemble.pairs_per_lane" (1 or 2: i-tile of 256 or 512 bodies
  * per work unit), "ensemble.blocks_per_sm" (0 = as many as fit),
- * "ensemble.unroll" (2, 4 or 8: j-loop unroll of the force kernel) and
+ * "ensemble.unroll" (2, 4 or 8: j-loop unroll of the force kernel),
+ * "ensemble.uniform_mass" (1, the default: when every system has equal
+ * masses, pairs are weighted by r^-3 alone and each system's mass scales its
+ * sums once, in FP64; 0: the mass-weighted kernel) and
  * "ensemble.hold_after_reject" (1, the default: a system's step may not grow
  * right after a rejected step; 0: it may, up to 5x) and
  * "ensemble.pi_control" (1: PI step control on accepted steps, fewer

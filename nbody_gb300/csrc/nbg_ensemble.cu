@@ -117,13 +117,39 @@ __device__ __forceinline__ void pair2e(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f2_t 
     az = f2_fma(dz, s3, az);
 }
 
+// Equal masses within a system: the pair weight is r^-3 alone and the
+// system's mass scales the sums once, in FP64 (one packed multiply fewer).
+template <bool CLAMP>
+__device__ __forceinline__ void pair2e_uni(f2_t xj, f2_t yj, f2_t zj, f2_t xi, f2_t yi, f2_t zi,
+                                           f2_t eps2, f2_t& ax, f2_t& ay, f2_t& az) {
+    const f2_t dx = f2_sub(xj, xi);
+    const f2_t dy = f2_sub(yj, yi);
+    const f2_t dz = f2_sub(zj, zi);
+    f2_t r2 = f2_fma(dz, dz, eps2);
+    r2 = f2_fma(dy, dy, r2);
+    r2 = f2_fma(dx, dx, r2);
+    float r2a, r2b;
+    f2_unpack(r2, r2a, r2b);
+    if (CLAMP) {
+        r2a = fmaxf(r2a, 1e-8f);
+        r2b = fmaxf(r2b, 1e-8f);
+    }
+    const f2_t inv = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
+    const f2_t s3 = f2_mul(f2_mul(inv, inv), inv);
+    ax = f2_fma(dx, s3, ax);
+    ay = f2_fma(dy, s3, ay);
+    az = f2_fma(dz, s3, az);
+}
+
 // Persistent direct sum over all systems.  Each lane holds G packed pairs
-// (2G i-bodies: slots r = 0 .. 2G-1 at i0 + r * 128 + threadIdx.x).
-template <bool CLAMP, int G, int U = 4>
+// (2G i-bodies: slots r = 0 .. 2G-1 at i0 + r * 128 + threadIdx.x).  UNI:
+// every system has equal masses, sys_mass[s] its mass.
+template <bool CLAMP, int G, int U = 4, bool UNI = false>
 __global__ void __launch_bounds__(kEnsThreads)
 ens_force_kernel(const Body2* __restrict__ bodies, const long long* __restrict__ off,
                  const int* __restrict__ cnt, const EnsUnit* __restrict__ units, int nunits,
-                 unsigned* __restrict__ counter, double* __restrict__ acc, size_t B, float eps2v) {
+                 unsigned* __restrict__ counter, double* __restrict__ acc, size_t B, float eps2v,
+                 const double* __restrict__ sys_mass) {
     __shared__ __align__(16) Body2 tile[kEnsTile];
     __shared__ int next_unit;
     const f2_t eps2 = f2_pack(eps2v, eps2v);
@@ -180,8 +206,14 @@ ens_force_kernel(const Body2* __restrict__ bodies, const long long* __restrict__
                 const f2_t xj = f2_pack(p0.x, p0.y), yj = f2_pack(p0.z, p0.w);
                 const f2_t zj = f2_pack(p1.x, p1.y), mj = f2_pack(p1.z, p1.w);
 #pragma unroll
-                for (int g = 0; g < G; ++g)
-                    pair2e<CLAMP>(xj, yj, zj, mj, xi[g], yi[g], zi[g], eps2, ax[g], ay[g], az[g]);
+                for (int g = 0; g < G; ++g) {
+                    if constexpr (UNI)
+                        pair2e_uni<CLAMP>(xj, yj, zj, xi[g], yi[g], zi[g], eps2, ax[g], ay[g],
+                                          az[g]);
+                    else
+                        pair2e<CLAMP>(xj, yj, zj, mj, xi[g], yi[g], zi[g], eps2, ax[g], ay[g],
+                                      az[g]);
+                }
             }
 #pragma unroll
             for (int g = 0; g < G; ++g) {
@@ -198,12 +230,13 @@ ens_force_kernel(const Body2* __restrict__ bodies, const long long* __restrict__
             if (l0 < n || l1 < n) {
                 const f2_t hh[3] = {hx[g], hy[g], hz[g]};
                 const f2_t ll[3] = {lx[g], ly[g], lz[g]};
+                const double w = UNI ? sys_mass[un.sys] : 1.0;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     f2_unpack(hh[c], h0, h1);
                     f2_unpack(ll[c], q0, q1);
-                    if (l0 < n) acc[c * B + o + l0] = (double)h0 + (double)q0;
-                    if (l1 < n) acc[c * B + o + l1] = (double)h1 + (double)q1;
+                    if (l0 < n) acc[c * B + o + l0] = w * ((double)h0 + (double)q0);
+                    if (l1 < n) acc[c * B + o + l1] = w * ((double)h1 + (double)q1);
                 }
             }
         }
@@ -300,6 +333,8 @@ struct nbg_ensemble {
     double* y = nullptr;
     double* ynew = nullptr;
     double* mass = nullptr;
+    double* sys_mass = nullptr;  // [nsys] each system's mass when all are uniform
+    bool all_uniform = false;    // every system has equal masses
     double* k[kStagesRK] = {nullptr};
     Body2* bodies = nullptr;
     double* dt = nullptr;
@@ -321,20 +356,31 @@ struct nbg_ensemble {
 namespace {
 
 using EnsForce = void (*)(const Body2*, const long long*, const int*, const EnsUnit*, int,
-                          unsigned*, double*, size_t, float);
+                          unsigned*, double*, size_t, float, const double*);
 
-template <bool CLAMP, int G>
+template <bool CLAMP, int G, bool UNI>
 EnsForce ens_pick_unroll(int64_t u) {
-    return u >= 8 ? ens_force_kernel<CLAMP, G, 8>
-                  : u <= 2 ? ens_force_kernel<CLAMP, G, 2> : ens_force_kernel<CLAMP, G, 4>;
+    return u >= 8 ? ens_force_kernel<CLAMP, G, 8, UNI>
+                  : u <= 2 ? ens_force_kernel<CLAMP, G, 2, UNI> : ens_force_kernel<CLAMP, G, 4, UNI>;
 }
 
-// "ensemble.unroll": unroll of the force kernel's j loop (2, 4 or 8)
+template <bool UNI>
+EnsForce ens_pick_g(bool clamp, int G, int64_t u) {
+    return clamp ? (G == 1 ? ens_pick_unroll<true, 1, UNI>(u) : ens_pick_unroll<true, 2, UNI>(u))
+                 : (G == 1 ? ens_pick_unroll<false, 1, UNI>(u) : ens_pick_unroll<false, 2, UNI>(u));
+}
+
+bool ens_uniform(const nbg_ensemble* s) {
+    return s->all_uniform && s->eng->tune_get("ensemble.uniform_mass", 1) != 0;
+}
+
+// "ensemble.unroll": unroll of the force kernel's j loop (2, 4 or 8);
+// "ensemble.uniform_mass" (1, the default): the equal-mass kernel when every
+// system has equal masses
 EnsForce ens_pick(const nbg_ensemble* s) {
     const bool clamp = !(s->p.softening > 0.0);
     const int64_t u = s->eng->tune_get("ensemble.unroll", 4);
-    return clamp ? (s->G == 1 ? ens_pick_unroll<true, 1>(u) : ens_pick_unroll<true, 2>(u))
-                 : (s->G == 1 ? ens_pick_unroll<false, 1>(u) : ens_pick_unroll<false, 2>(u));
+    return ens_uniform(s) ? ens_pick_g<true>(clamp, s->G, u) : ens_pick_g<false>(clamp, s->G, u);
 }
 
 // Work units and launch shape from the tuning keys (the i-block tile of
@@ -384,7 +430,7 @@ nbg_status ens_enqueue_force(nbg_ensemble* s) {
     NBG_LAUNCHED(e, "ens_stage_kernel");
     ens_pick(s)<<<s->force_grid, kEnsThreads, 0, e->stream>>>(
         s->bodies, s->off, s->cnt, s->units, s->nunits, s->counters, s->k[0] + 3 * s->B, s->B,
-        (float)(s->p.softening * s->p.softening));
+        (float)(s->p.softening * s->p.softening), s->sys_mass);
     NBG_LAUNCHED(e, "ens_force_kernel");
     return NBG_OK;
 }
@@ -405,7 +451,8 @@ nbg_status ens_enqueue_step(nbg_ensemble* s) {
         NBG_LAUNCHED(e, "ens_stage_kernel");
         ProfScope ps(e, NBG_K_DIRECT);
         kern<<<grid, kEnsThreads, 0, e->stream>>>(s->bodies, s->off, s->cnt, s->units, s->nunits,
-                                                  s->counters + st, s->k[st] + 3 * s->B, s->B, eps2);
+                                                  s->counters + st, s->k[st] + 3 * s->B, s->B, eps2,
+                                                  s->sys_mass);
         NBG_LAUNCHED(e, "ens_force_kernel");
     }
     ens_error_kernel<<<gv, 256, 0, e->stream>>>(s->y, s->sys, s->dt, kp, s->B, s->ynew, s->err);
@@ -421,7 +468,7 @@ nbg_status ens_enqueue_step(nbg_ensemble* s) {
 }
 
 void ens_free(nbg_ensemble* s) {
-    void* ptrs[] = {s->off, s->cnt, s->sys, s->y, s->ynew, s->mass, s->bodies, s->dt, s->t,
+    void* ptrs[] = {s->off, s->cnt, s->sys, s->y, s->ynew, s->mass, s->sys_mass, s->bodies, s->dt, s->t,
                     s->err, s->accepted, s->rejected, s->decision, s->err_prev, s->units,
                     s->counters};
     for (void* p : ptrs) cudaFree(p);
@@ -520,6 +567,7 @@ nbg_status nbg_ensemble_init(nbg_ensemble* s, size_t nsys, const uint32_t* count
     NBG_CUDA(e, cudaMalloc(&s->y, B6 * sizeof(double)));
     NBG_CUDA(e, cudaMalloc(&s->ynew, B6 * sizeof(double)));
     NBG_CUDA(e, cudaMalloc(&s->mass, B * sizeof(double)));
+    NBG_CUDA(e, cudaMalloc(&s->sys_mass, nsys * sizeof(double)));
     for (int i = 0; i < kStagesRK; ++i) NBG_CUDA(e, cudaMalloc(&s->k[i], B6 * sizeof(double)));
     NBG_CUDA(e, cudaMalloc(&s->bodies, B * sizeof(Body2)));
     NBG_CUDA(e, cudaMalloc(&s->dt, nsys * sizeof(double)));
@@ -546,6 +594,18 @@ nbg_status nbg_ensemble_init(nbg_ensemble* s, size_t nsys, const uint32_t* count
     NBG_CUDA(e, cudaMemcpy(s->sys, hsys.data(), B * sizeof(int), cudaMemcpyHostToDevice));
     NBG_CUDA(e, cudaMemcpy(s->y, h.data(), B6 * sizeof(double), cudaMemcpyHostToDevice));
     NBG_CUDA(e, cudaMemcpy(s->mass, mass, B * sizeof(double), cudaMemcpyHostToDevice));
+    // equal masses within every system select the kernel that scales by the
+    // system's mass once
+    std::vector<double> smass(nsys);
+    s->all_uniform = true;
+    for (size_t sI = 0; sI < nsys; ++sI) {
+        const double* m0 = mass + s->h_off[sI];
+        smass[sI] = m0[0];
+        for (int k = 1; k < s->h_cnt[sI] && s->all_uniform; ++k)
+            s->all_uniform = m0[k] == m0[0];
+    }
+    NBG_CUDA(e, cudaMemcpy(s->sys_mass, smass.data(), nsys * sizeof(double),
+                           cudaMemcpyHostToDevice));
     NBG_CUDA(e, cudaMemcpy(s->dt, dt0.data(), nsys * sizeof(double), cudaMemcpyHostToDevice));
     NBG_CUDA(e, cudaMemcpy(s->t, t0.data(), nsys * sizeof(double), cudaMemcpyHostToDevice));
     NBG_CUDA(e, cudaMemset(s->accepted, 0, nsys * sizeof(unsigned)));

@@ -147,3 +147,37 @@ def test_ensemble_statistics_unsoftened_match_oracle(gpulib, oracle):
         ref = oracle.statistics(d.to_state(), d.mass)
         assert np.allclose(st[k], ref, rtol=1e-10, atol=1e-13)
     ens.close()
+
+
+def test_ensemble_uniform_mass_kernel(gpulib, oracle):
+    """Equal masses in every system select the kernel that scales each
+    system's sums by its mass once; it agrees with the mass-weighted kernel to
+    FP32 rounding.  One system with unequal masses keeps the general kernel
+    for all (results against the oracle)."""
+    sizes = [64, 300, 1000, 2048]
+    sy = _systems(sizes, seed=9)
+    out = []
+    for uni in (1, 0):
+        ens = Ensemble(softening=1e-3)
+        ens.tune_set("ensemble.uniform_mass", uni)
+        ens.init(sy)
+        out.append(ens.fcompute())
+        ens.close()
+    B = sum(sizes)
+    a_u, a_g = (o[3 * B:].reshape(3, B).T for o in out)
+    rel = np.linalg.norm(a_u - a_g, axis=1) / np.linalg.norm(a_g, axis=1)
+    assert np.sqrt(np.mean(rel ** 2)) < 5e-7 and rel.max() < 1e-4
+    mixed = sy[:2] + _systems([500], seed=4, kind="cube")
+    ens = Ensemble(softening=1e-3)
+    ens.init(mixed)
+    f = ens.fcompute()
+    ens.close()
+    Bm = sum(d.get_count() for d in mixed)
+    a = f[3 * Bm:].reshape(3, Bm).T
+    off = 0
+    for d in mixed:
+        n = d.get_count()
+        ref = oracle.accel_rows(d.to_state(), d.mass, 1e-3)
+        r = np.linalg.norm(a[off:off + n] - ref, axis=1) / np.linalg.norm(ref, axis=1)
+        assert np.sqrt(np.mean(r ** 2)) < 1e-5
+        off += n
