@@ -570,6 +570,11 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None, train_samples: int 
         "hilbert_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d),
         "hilbert_theta_0.9": lambda: bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d),
         "hilbert_lambda_2.5": lambda: bench_bh(n_bh, 2.5, False, rows, a_ref, d),
+        # 128-body groups: half the traversal per body, larger boxes
+        "hilbert_theta_0.5_group128": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d,
+                                                       tune={"bh.group": 128}),
+        "hilbert_theta_0.9_group128": lambda: bench_bh(n_bh, 1.0 / 0.9, False, rows, a_ref, d,
+                                                       tune={"bh.group": 128}),
         "morton_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, build=1),
         "quadrupole_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d, order=2,
                                                  build=0),

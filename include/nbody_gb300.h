@@ -271,7 +271,8 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       sums by the mass once, in FP64; 0: the general kernel),
  *       "bh.walk" (1: group walk with interaction lists, 0: warp-coherent
  *       stackless walk) for the mixed-precision Barnes-Hut path,
- *       "bh.group" (64 or 32 bodies per warp in the group walk),
+ *       "bh.group" (64 (default), 32 or 128 bodies per warp in the group
+ *       walk; 128 with monopole cells only),
  *       "bh.build" (0: the reference's kd-median tree, always for FP64;
  *       mixed precision: 1 leaves in Morton order, 2 in Hilbert order (the
  *       default), every node the two halves of its range -- one sort

@@ -1053,7 +1053,12 @@ nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
         const int stack_cap = group_stack_cap(t->levels);
         size_t smem = sizeof(GroupSmem) + (order == 2 ? sizeof(QuadLists) : 0) +
                       (size_t)kGWWarps * stack_cap * sizeof(int);
-        const int bpl = (e->tune_get("bh.group", 64) >= 64 && n >= 64) ? 2 : 1;
+        // "bh.group": 32, 64 (default) or 128 bodies per warp group (128:
+        // monopole cells only, accumulators in shared memory, 4 CTAs per SM)
+        const bool frozen_req = e->tune_get("bh.freeze_within_step", 0) != 0;
+        const int64_t gsz = e->tune_get("bh.group", 64);
+        const int bpl = (gsz >= 128 && n >= 128 && order == 1 && !frozen_req) ? 4
+                        : (gsz >= 64 && n >= 64) ? 2 : 1;
         // 64-body groups keep their accumulators in shared memory by default
         // and run 5 CTAs per SM ("bh.acc_smem" = 0: registers, 4 CTAs)
         const bool acc_smem = bpl == 2 && order == 1 && e->tune_get("bh.acc_smem", 1) != 0;
@@ -1075,7 +1080,11 @@ nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
                              "(64-body groups, monopole cells)");
 #define NBG_GW(C, B) (wb >= 8 ? bh_group_walk_kernel<C, 8, B, 1> : wb >= 6 ? bh_group_walk_kernel<C, 6, B, 1> \
                       : wb >= 5 ? bh_group_walk_kernel<C, 5, B, 1> : bh_group_walk_kernel<C, 4, B, 1>)
-        if (frozen) {
+        if (bpl == 4) {
+            smem += (size_t)kGWThreads * 6 * 4 * sizeof(f2_t);
+            kern = clamp ? bh_group_walk_kernel<true, 4, 4, 1, 2, true>
+                         : bh_group_walk_kernel<false, 4, 4, 1, 2, true>;
+        } else if (frozen) {
             // the default build keeps its accumulators in shared memory, and
             // the frozen walk three residual lists per warp after them
             smem += (size_t)kGWThreads * 6 * 2 * sizeof(f2_t) +
@@ -1133,7 +1142,8 @@ nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
             const unsigned ratio = (unsigned)std::max<int64_t>(e->tune_get("bh.test_cap_ratio", 2), 1);
             const int samples = std::min(warps, kCapSamples);  // both powers of two
             const size_t csmem = (size_t)kCapSamples * stack_cap * sizeof(int);
-            auto capk = bpl == 2 ? bh_test_cap_kernel<2> : bh_test_cap_kernel<1>;
+            auto capk = bpl == 4 ? bh_test_cap_kernel<4>
+                        : bpl == 2 ? bh_test_cap_kernel<2> : bh_test_cap_kernel<1>;
             NBG_CUDA(e, cudaFuncSetAttribute(capk, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)csmem));
             // the cap counts acceptance tests: against the step build's
@@ -1158,6 +1168,8 @@ nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
         NBG_LAUNCHED(e, "bh_group_walk_kernel");
         auto fb = frozen
             ? (clamp ? bh_body_walk_kernel<true, 2, 1, true> : bh_body_walk_kernel<false, 2, 1, true>)
+            : bpl == 4
+            ? (clamp ? bh_body_walk_kernel<true, 4, 1> : bh_body_walk_kernel<false, 4, 1>)
             : order == 2
             ? (clamp ? (bpl == 2 ? bh_body_walk_kernel<true, 2, 2> : bh_body_walk_kernel<true, 1, 2>)
                      : (bpl == 2 ? bh_body_walk_kernel<false, 2, 2> : bh_body_walk_kernel<false, 1, 2>))

@@ -100,6 +100,7 @@ extern "C" nbg_status nbg_autotune(nbg_engine* e, int reps, char* report, size_t
             cands.push_back({{"bh.walk", 1}, {"bh.group", 64}, {"bh.walk_blocks", 4}, {"bh.acc_smem", 0},
                              {"bh.eval_unroll", u}});
         for (int b : {6, 8}) cands.push_back({{"bh.walk", 1}, {"bh.group", 32}, {"bh.walk_blocks", b}});
+        cands.push_back({{"bh.walk", 1}, {"bh.group", 128}});
         cands.push_back({{"bh.walk", 0}});
     } else {
         cands = direct_candidates();

@@ -307,8 +307,7 @@ def test_bh_hilbert_clustered_and_degenerate(make_engine, oracle):
     assert np.all(f[3 * n:] == 0.0)
 
 
-@pytest.mark.parametrize("group", [64, 32])
-@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("group,order", [(64, 1), (64, 2), (32, 1), (32, 2), (128, 1)])
 def test_bh_body_walk_fallback(make_engine, oracle, group, order):
     """A group walk that exceeds bh.test_cap node tests hands its bodies to
     the per-body walk.  With a cap of one test every group does: the forces
@@ -453,3 +452,28 @@ def test_bh_freeze_within_step(make_engine, oracle):
     _f(pl, y1)
     _, i2p = pl.bh_counters()
     assert i2 == i2p and close(f2, f1p)
+
+
+@pytest.mark.parametrize("n", [128, 4096, 1 << 16])
+def test_bh_group128_as_accurate_as_group64(make_engine, oracle, n):
+    """128-body groups (bh.group = 128) accept a refinement of every body's
+    per-body set, like 64-body groups: on the default Hilbert tree the error
+    against the FP64 direct sum is at most the 64-body walk's (their larger
+    boxes open more cells), and a full tree of one group is a direct sum."""
+    d = NBodyData.plummer(n, seed=17)
+    y = d.to_state()
+    rows = np.arange(n) if n <= 4096 else np.random.default_rng(5).choice(n, 1024, replace=False)
+    a_ref = oracle.accel_rows(y, d.mass, 1e-3, rows=rows)
+    errs = {}
+    for g in (64, 128):
+        e = make_engine(algo="bh", precision="mixed", softening=1e-3,
+                        distance_to_node_radius_ratio=2.0)
+        e.tune_set("bh.group", g)
+        assert e.init(d)
+        f = _f(e, y)
+        assert np.array_equal(f[:3 * n], y[3 * n:])
+        errs[g] = _rel(f[3 * n:].reshape(3, n).T[rows], a_ref)
+    if n == 128:
+        assert errs[128].max() < 1e-5
+    assert np.quantile(errs[128], 0.99) <= 1.05 * np.quantile(errs[64], 0.99)
+    assert np.median(errs[128]) <= 1.05 * np.median(errs[64])
