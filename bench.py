@@ -555,11 +555,11 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None, train_samples: int 
         r["training"] = fit
         return r
 
-    def learned_raw_case():
+    def learned_raw_case(tune=None):
         if "w" not in learned_w:
             learned_w["w"] = train_correction(samples=train_samples)[0]
         return bench_bh(n_bh, 1.0 / 0.9, True, rows, a_ref, d, weights=learned_w["w"],
-                        judge=False)
+                        judge=False, tune=tune)
 
     suite = {
         # the reference's kd-median tree at the reference's opening ratios,
@@ -605,8 +605,11 @@ def run_bh_suite(rank: int, n_bh: int = 1 << 20, cases=None, train_samples: int 
         "refit_rate4_hilbert_theta_0.5": lambda: bench_bh(n_bh, 2.0, False, rows, a_ref, d,
                                                           calls=8, build_rate=4),
         "learned_theta_0.9": learned_case,
-        # the learned walk alone (no judge, no fallback)
+        # the learned walk alone (no judge, no fallback): the default group
+        # walk with the network on the tcgen05 tensor cores, and the
+        # warp-coherent per-body walk with one mma.sync batch per band cell
         "learned_walk_theta_0.9": learned_raw_case,
+        "learned_coherent_walk_theta_0.9": lambda: learned_raw_case({"learned.walk": 0}),
         "accuracy_frontier": lambda: accuracy_frontier(n_bh, rows, a_ref, d),
         "rkdp_theta_0.5": lambda: bh_rkdp_run(n_bh, d),
         # the same run with a tree rebuilt at every stage (the reference's
@@ -669,7 +672,7 @@ def bh_summary(bh):
                                         "speedup_vs_reference_method":
                                             _r(b["speedup_vs_reference_method"])}
     for k in ("hilbert_theta_0.5", "plain_theta_0.5", "hilbert_theta_0.9", "learned_theta_0.9",
-              "learned_walk_theta_0.9", "fp64_theta_0.5"):
+              "learned_walk_theta_0.9", "learned_coherent_walk_theta_0.9", "fp64_theta_0.5"):
         if k in bh and "bodies_per_s" in bh[k]:
             out[k] = {x: _r(bh[k][x]) for x in ("ms_per_fcompute", "bodies_per_s", "p50", "p99")}
             if "judge" in bh[k]:

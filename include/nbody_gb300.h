@@ -196,9 +196,14 @@ nbg_status nbg_bh_fallback_groups(nbg_engine* e, uint64_t* groups);
  * u/|u|, Q u/|u| and the mass-centre offset o of the features (g = c0 u/|u|
  * + c1 Q u/|u| + c2 o); nbg_learn_predict returns c.  Used when
  * nbg_params.learned = 1 (Barnes-Hut, mixed precision); tuning keys:
- * "learned.group" one sample per (body, cell) (0, default) or per (warp,
- * cell) at the warp centroid (1); "learned.weighted" (0 default, 1: training
- * loss weighted by the cell's force scale (m / s^2)^2).
+ * "learned.walk" 1 (default): the default group walk (64-body groups)
+ * records each group's band cells and the network evaluates the band
+ * (body, cell) rows in 128-row tiles on the tcgen05 tensor cores, the
+ * per-body sums taken in a fixed order; 0: the warp-coherent per-body walk
+ * with one mma.sync batch per band cell; "learned.group" one sample per
+ * (body, cell) (0, default) or per (warp, cell) at the warp centroid (1, on
+ * the per-body walk); "learned.weighted" (0 default, 1: training loss
+ * weighted by the cell's force scale (m / s^2)^2).
  * Judge and fallback: at the first fcompute of every engine step a direct
  * sum on a seeded sample of bodies ("learned.judge_samples", default 4096,
  * rounded down to a power of two; "learned.judge_seed", default 1) measures
@@ -237,6 +242,16 @@ nbg_status nbg_learn_loss_grad(nbg_engine* e, const float* x, const float* t, si
 /* Network outputs g (x [count][16] -> out [count][3]) with the inference
  * routine of the walk. */
 nbg_status nbg_learn_predict(nbg_engine* e, const float* x, size_t count, float* out);
+/* The same outputs from the tensor-core (tcgen05) inference of
+ * "learned.walk" = 1: 128-row tiles, BF16 operands in shared memory, FP32
+ * accumulators in tensor memory.  count <= 2^30. */
+nbg_status nbg_learn_predict_tc(nbg_engine* e, const float* x, size_t count, float* out);
+/* For checks of the tcgen05 layouts: each row's tensor-memory accumulators
+ * of that forward pass, acc [count][144]: the first layer's D1 = X W1
+ * (0..63), the second layer's D2 = GELU(D1 + b1) W2 (64..127) and the
+ * third layer's D3 = GELU(D2 + b2) W3 (128..143; 131..143 zero), biases
+ * not added. */
+nbg_status nbg_learn_tc_accumulators(nbg_engine* e, const float* x, size_t count, float* acc);
 /* The judge's figures: out[0] engine step judged last, [1] p50 and [2] p99
  * relative error of the learned forces, [3] p50 and [4] p99 of the plain
  * walk at the tight ratio, [5] RMS learned, [6] RMS plain, [7] 1 when that

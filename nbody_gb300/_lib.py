@@ -37,7 +37,7 @@ EXPORTS = [
     "nbg_bh_counters", "nbg_learn_param_count", "nbg_learn_set_weights",
     "nbg_learn_get_weights", "nbg_learn_init_weights", "nbg_learn_generate",
     "nbg_learn_sample_count", "nbg_learn_read_samples", "nbg_learn_clear_samples",
-    "nbg_learn_train", "nbg_learn_loss_grad", "nbg_tree_leaves", "nbg_learn_predict", "nbg_statistics",
+    "nbg_learn_train", "nbg_learn_loss_grad", "nbg_tree_leaves", "nbg_learn_predict", "nbg_learn_predict_tc", "nbg_learn_tc_accumulators", "nbg_statistics",
     "nbg_ensemble_params_default", "nbg_ensemble_create", "nbg_ensemble_destroy",
     "nbg_ensemble_last_error", "nbg_ensemble_init", "nbg_ensemble_step",
     "nbg_ensemble_synchronize", "nbg_ensemble_status", "nbg_ensemble_get_state",
@@ -163,6 +163,8 @@ def load() -> C.CDLL:
     _proto(lib, "nbg_learn_loss_grad", i32, vp, fp, fp, sz, dp, fp)
     _proto(lib, "nbg_tree_leaves", i32, vp, ip)
     _proto(lib, "nbg_learn_predict", i32, vp, fp, sz, fp)
+    _proto(lib, "nbg_learn_predict_tc", i32, vp, fp, sz, fp)
+    _proto(lib, "nbg_learn_tc_accumulators", i32, vp, fp, sz, fp)
     _proto(lib, "nbg_learn_judge_stats", i32, vp, dp, sz)
     _proto(lib, "nbg_learn_band_rows", i32, vp, C.POINTER(u64))
     _proto(lib, "nbg_statistics", i32, vp, vp, dp)

@@ -195,10 +195,6 @@ bh_walk_mixed_kernel(const double* __restrict__ y, double* __restrict__ f, int n
 // per-body walk at the same ratio.
 constexpr int kGWWarps = 4;
 constexpr int kGWThreads = kGWWarps * 32;
-// Stack entries per warp: 48 per tree level plus 32 (a step pops 16 entries
-// and pushes at most 32), set per launch from the tree depth; the deepest
-// stack of every launch is recorded in counters[2].
-constexpr int kGWStackPerLevel = 48;
 constexpr int kGWList = 256;    // interaction entries per warp
 
 struct GroupSmem {  // followed by the stacks, kGWWarps x stack_cap ints
@@ -207,8 +203,6 @@ struct GroupSmem {  // followed by the stacks, kGWWarps x stack_cap ints
     float lz[kGWWarps][kGWList];
     float lm[kGWWarps][kGWList];
 };
-
-inline int group_stack_cap(int levels) { return kGWStackPerLevel * (levels + 1) + 32; }
 
 // groups whose node tests set the group walk's test cap (one warp each, one block)
 constexpr int kCapSamples = 32;
@@ -315,7 +309,11 @@ __device__ __forceinline__ void group_pair_lo(f2_t xj, f2_t yj, f2_t zj, f2_t mj
 // SMACC: the per-body two-sum accumulators (6 BPL packed values per lane)
 // live in shared memory instead of registers; they are touched once per list
 // evaluation, and the registers they free allow more resident warps.
-template <bool CLAMP, int BPL, int ORDER, int EUNR, bool SMACC, bool FROZEN = false>
+// EMIT: cells accepted with the group box's nearest point inside the tight
+// ratio (the learned correction's band) are recorded in t.cand; a group
+// with more than t.cand_cap of them is handed to the per-body walk.
+template <bool CLAMP, int BPL, int ORDER, int EUNR, bool SMACC, bool FROZEN = false,
+          bool EMIT = false>
 __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, double* __restrict__ f,
                                                int n, float eps2v, const TreeState& t,
                                                int stack_cap, unsigned* err,
@@ -402,7 +400,7 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
     unsigned long long tests = 0, inter = 0;
     if (lane == 0) stack[0] = 0;
     __syncwarp();
-    int sp = 1, lc = 0, peak = 1;
+    int sp = 1, lc = 0, peak = 1, ec = 0;
     bool overflow = false, abandoned = false;
     const unsigned long long test_cap = t.test_cap != 0 ? t.test_cap : t.cap_state[0];
 
@@ -525,7 +523,7 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
         __syncwarp();
         sp -= k;
         const bool valid = lane < 2 * k && c != 0;
-        bool accept = false, open = false;
+        bool accept = false, open = false, band = false;
         // issued before a full list is evaluated, which covers their latency;
         // lanes past the popped entries read record 0 (unused, zeroed), and
         // leaves' second moments are zero
@@ -549,6 +547,7 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
                 const float dmin2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
                 accept = dmin2 > nda.w;
                 open = !accept;
+                if constexpr (EMIT) band = accept && dmin2 <= nda.w * t.band2;
             }
         }
         // every popped entry stands for two tested children, except the root's
@@ -557,6 +556,15 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
         if (tests > test_cap) {  // a group spread over much of the system:
             abandoned = true;      // its bodies are walked one by one instead
             break;
+        }
+        if constexpr (EMIT) {
+            const unsigned bm = __ballot_sync(0xffffffffu, band);
+            if (ec + __popc(bm) > t.cand_cap) {  // walked body by body instead
+                abandoned = true;
+                break;
+            }
+            if (band) t.cand[(size_t)gw * t.cand_cap + ec + __popc(bm & lt)] = c;
+            ec += __popc(bm);
         }
         // cells with moments go to the quadrupole list (ORDER 2), the rest
         // (leaves, or every node for ORDER 1) to the monopole list
@@ -616,6 +624,9 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
         atomicAdd(&t.counters[0], tests);
         atomicMax(&t.counters[2], (unsigned long long)peak);
     }
+    if constexpr (EMIT) {
+        if (lane == 0) t.cand_n[gw] = abandoned ? 0u : (unsigned)ec;
+    }
     if (abandoned) {
         if (lane == 0) {
             t.fb_list[atomicAdd(t.fb_count, 1u)] = gw;
@@ -651,7 +662,7 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
 // leaving a partial wave.  A group's forces do not depend on which warp
 // computes it.
 template <bool CLAMP, int MINB, int BPL, int ORDER, int EUNR = 2, bool SMACC = false,
-          bool FROZEN = false>
+          bool FROZEN = false, bool EMIT = false>
 __global__ void __launch_bounds__(kGWThreads, MINB)
 bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n, float eps2v,
                      TreeState t, int stack_cap, unsigned* err) {
@@ -660,8 +671,8 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
     const int groups = n / (32 * BPL);
     int gw = blockIdx.x * kGWWarps + (threadIdx.x >> 5);
     while (gw < groups) {
-        group_walk_one<CLAMP, BPL, ORDER, EUNR, SMACC, FROZEN>(y, f, n, eps2v, t, stack_cap, err,
-                                                              smem_raw, gw);
+        group_walk_one<CLAMP, BPL, ORDER, EUNR, SMACC, FROZEN, EMIT>(y, f, n, eps2v, t, stack_cap,
+                                                                    err, smem_raw, gw);
         int next = 0;
         if (lane == 0) next = (int)atomicAdd(&t.fb_count[1], 1u);
         gw = gridDim.x * kGWWarps + __shfl_sync(0xffffffffu, next, 0);
@@ -1034,10 +1045,21 @@ nbg_status bh_fcompute(nbg_engine* e, uint64_t step, const double* y, double* f)
     return mixed_walk(e, y, f);
 }
 
-nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
+namespace {
+nbg_status mixed_walk_impl(nbg_engine* e, const double* y, double* f, bool emit);
+}  // namespace
+
+// the emitting walk is one part of the learned walk, whose caller times it
+nbg_status mixed_walk(nbg_engine* e, const double* y, double* f, bool emit) {
+    if (emit) return mixed_walk_impl(e, y, f, true);
+    ProfScope ps(e, NBG_K_BH_WALK);
+    return mixed_walk_impl(e, y, f, false);
+}
+
+namespace {
+nbg_status mixed_walk_impl(nbg_engine* e, const double* y, double* f, bool emit) {
     const int n = (int)e->count;
     TreeState* t = e->tree;
-    ProfScope ps(e, NBG_K_BH_WALK);
     const float eps2 = (float)(e->params.softening * e->params.softening);
     const bool clamp = !(e->params.softening > 0.0);
     if (e->tune_get("bh.walk", 1) == 1 && n >= 32) {
@@ -1078,9 +1100,17 @@ nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
             return set_error(e, NBG_ERR_UNSUPPORTED,
                              "bh.freeze_within_step runs the default group walk only "
                              "(64-body groups, monopole cells)");
+        if (emit && (frozen || !(bpl == 2 && order == 1 && acc_smem)))
+            return set_error(e, NBG_ERR_UNSUPPORTED,
+                             "the learned correction on tensor cores runs on the default group "
+                             "walk only (64-body groups, monopole cells, no frozen acceptance)");
 #define NBG_GW(C, B) (wb >= 8 ? bh_group_walk_kernel<C, 8, B, 1> : wb >= 6 ? bh_group_walk_kernel<C, 6, B, 1> \
                       : wb >= 5 ? bh_group_walk_kernel<C, 5, B, 1> : bh_group_walk_kernel<C, 4, B, 1>)
-        if (bpl == 4) {
+        if (emit) {
+            smem += (size_t)kGWThreads * 6 * 2 * sizeof(f2_t);
+            kern = clamp ? bh_group_walk_kernel<true, 5, 2, 1, 2, true, false, true>
+                         : bh_group_walk_kernel<false, 5, 2, 1, 2, true, false, true>;
+        } else if (bpl == 4) {
             smem += (size_t)kGWThreads * 6 * 4 * sizeof(f2_t);
             kern = clamp ? bh_group_walk_kernel<true, 4, 4, 1, 2, true>
                          : bh_group_walk_kernel<false, 4, 4, 1, 2, true>;
@@ -1166,6 +1196,7 @@ nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
         }
         kern<<<blocks, kGWThreads, smem, e->stream>>>(y, f, n, eps2, *t, stack_cap, e->d_err);
         NBG_LAUNCHED(e, "bh_group_walk_kernel");
+        if (emit) return NBG_OK;
         auto fb = frozen
             ? (clamp ? bh_body_walk_kernel<true, 2, 1, true> : bh_body_walk_kernel<false, 2, 1, true>)
             : bpl == 4
@@ -1197,6 +1228,7 @@ nbg_status mixed_walk(nbg_engine* e, const double* y, double* f) {
     NBG_LAUNCHED(e, "bh_walk_mixed_kernel");
     return NBG_OK;
 }
+}  // namespace
 
 }  // namespace nbg
 

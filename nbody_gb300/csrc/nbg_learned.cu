@@ -29,40 +29,12 @@
 #include <cstring>
 #include <vector>
 
+#include "nbg_learned.cuh"
 #include "nbg_mlp.cuh"
 #include "nbg_ptx.cuh"
 #include "nbg_tree.cuh"
 
 namespace nbg {
-
-struct LearnState {
-    // model
-    float* w = nullptr;      // FP32 master parameters [kParams]
-    float* grad = nullptr;   // [kParams]
-    float* m1 = nullptr;     // Adam first moment
-    float* m2 = nullptr;     // Adam second moment
-    uint2* frag = nullptr;   // fragment-ordered BF16 weights [kFragWords]
-    float* bias = nullptr;   // padded biases [kBias]
-    double* loss = nullptr;  // [2] sum of squared error, sample count
-    int64_t adam_step = 0;
-    bool has_weights = false;
-    // training samples
-    float* x = nullptr;      // [cap][16]
-    float* t = nullptr;      // [cap][4]
-    int* meta = nullptr;     // [cap][2] (body, node) of the snapshot that made it
-    size_t count = 0, cap = 0;
-    // sample-generation scratch
-    int* pairs = nullptr;    // [cap][2]
-    unsigned long long* pair_count = nullptr;
-    double* mom = nullptr;   // [6][size] FP64 second moments of the current tree
-    size_t mom_size = 0;
-    // per-step judge (nbg_judge.cu): the step judged last, the step sent to
-    // the plain walk, counts, the last figures
-    bool judged_valid = false, plain_valid = false;
-    uint64_t judged_step = 0, plain_step = 0;
-    uint64_t judged = 0, fallbacks = 0;
-    JudgeResult last;
-};
 
 namespace {
 
@@ -127,57 +99,6 @@ __global__ void features_kernel(TreeState t, const double* mom, double lambda) {
         t.feat[3 * idx + 1] = f1;
         t.feat[3 * idx + 2] = f2;
     }
-}
-
-// The 16 features of (body at x, cell); dx = c - x (FP32, as the walk has it).
-__device__ __forceinline__ void make_features(float dx, float dy, float dz, float inv_s,
-                                              float4 f0, float4 f1, float4 f2, float feat[16]) {
-    const float ux = -dx * inv_s, uy = -dy * inv_s, uz = -dz * inv_s;
-    feat[0] = ux;
-    feat[1] = uy;
-    feat[2] = uz;
-    feat[3] = f0.x;
-    feat[4] = f0.y;
-    feat[5] = f0.z;
-    feat[6] = f0.w;
-    feat[7] = f1.x;
-    feat[8] = f1.y;
-    feat[9] = f1.z;
-    feat[10] = f1.w;
-    feat[11] = f2.x;
-    feat[12] = rsqrtf(fmaf(ux, ux, fmaf(uy, uy, uz * uz)));
-    feat[13] = f2.y;
-    feat[14] = f2.z;
-    feat[15] = f2.w;
-}
-
-// Equivariant output head: the network's three outputs are coefficients of
-// vectors that turn with the cell and the body -- the body direction u/|u|,
-// the quadrupole applied to it Q u/|u|, and the mass-centre offset o:
-//     g = c0 u/|u| + c1 Q u/|u| + c2 o.
-// The exact quadrupole correction has this form, and a bias of the network
-// can no longer point the same way for every cell around a body (where it
-// would add up instead of cancelling).  basis[i] is the i-th vector.
-__device__ __forceinline__ void head_basis(const float feat[16], float basis[3][3]) {
-    const float iu = feat[12];
-    const float ux = feat[0] * iu, uy = feat[1] * iu, uz = feat[2] * iu;
-    // Q = [[xx, xy, xz], [xy, yy, yz], [xz, yz, zz]], feat[3..8] = xx, yy, zz, xy, xz, yz
-    basis[0][0] = ux;
-    basis[0][1] = uy;
-    basis[0][2] = uz;
-    basis[1][0] = fmaf(feat[3], ux, fmaf(feat[6], uy, feat[7] * uz));
-    basis[1][1] = fmaf(feat[6], ux, fmaf(feat[4], uy, feat[8] * uz));
-    basis[1][2] = fmaf(feat[7], ux, fmaf(feat[8], uy, feat[5] * uz));
-    basis[2][0] = feat[13];
-    basis[2][1] = feat[14];
-    basis[2][2] = feat[15];
-}
-
-__device__ __forceinline__ void apply_head(const float feat[16], const float c[3], float g[3]) {
-    float b[3][3];
-    head_basis(feat, b);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) g[k] = fmaf(c[0], b[0][k], fmaf(c[1], b[1][k], c[2] * b[2][k]));
 }
 
 // ---------------------------------------------------------------------------
@@ -827,8 +748,10 @@ nbg_status rebuild_frags(nbg_engine* e) {
     LearnState* L = e->learn;
     make_frags_kernel<<<kTiles, 32, 0, e->stream>>>(L->w, L->frag, L->bias);
     NBG_LAUNCHED(e, "make_frags_kernel");
-    return NBG_OK;
+    return tc_rebuild_weights(e);
 }
+
+}  // namespace
 
 // node features of the current tree (after tree_build / tree_refit)
 nbg_status tree_features(nbg_engine* e) {
@@ -858,6 +781,8 @@ nbg_status tree_features(nbg_engine* e) {
     return NBG_OK;
 }
 
+namespace {
+
 size_t train_smem() { return sizeof(TrainSmem); }
 size_t walk_smem() { return sizeof(WalkSmem); }
 
@@ -871,6 +796,7 @@ void learn_destroy(nbg_engine* e) {
     void* ptrs[] = {L->w, L->grad, L->m1, L->m2, L->frag, L->bias, L->loss,
                     L->x, L->t, L->meta, L->pairs, L->pair_count, L->mom};
     for (void* p : ptrs) cudaFree(p);
+    learned_tc_free(L);
     delete L;
     e->learn = nullptr;
 }
@@ -883,6 +809,12 @@ nbg_status learned_walk(nbg_engine* e, const double* y, double* f) {
     if (s != NBG_OK) return s;
     TreeState* t = e->tree;
     const int n = (int)e->count;
+    // "learned.walk": 1 (default) the group walk with the network on the
+    // tcgen05 tensor cores (nbg_learned_tc.cu); 0 the warp-coherent per-body
+    // walk below, one mma.sync batch per band cell
+    if (e->tune_get("learned.walk", 1) == 1 && e->tune_get("learned.group", 0) == 0 &&
+        e->tune_get("bh.walk", 1) == 1 && n >= 64)
+        return learned_tc_walk(e, y, f);
     const double lam_l = e->params.distance_to_node_radius_ratio;
     const double lam_t = e->params.learned_tight_ratio;
     const float band2 = (float)((lam_t / lam_l) * (lam_t / lam_l));

@@ -62,6 +62,14 @@ struct TreeState {
 
     // learned-correction node features (quadrupole, spread), see nbg_learned.cu
     float4* feat = nullptr;   // [3][size] or null
+    // the group walk's band cells for the learned correction on tensor cores
+    // (set only while the learned path runs it): every cell a 64-body group
+    // accepts at lambda_l whose mass centre is within the tight ratio of the
+    // group's box (d_min^2 <= crit2 band2, band2 = (lambda_t / lambda_l)^2)
+    int* cand = nullptr;          // [groups][cand_cap]
+    unsigned* cand_n = nullptr;   // [groups]
+    int cand_cap = 0;
+    float band2 = 0.f;
 
     // quadrupole walk records (nbg_bh.cu): second central mass moments M
     // stored as S = -3 M, quad[2 idx] = (Sxx, Syy, Szz, tr S / 2),
@@ -82,6 +90,13 @@ struct TreeState {
     unsigned long long* cap_state = nullptr; // [1]
     unsigned long long test_cap = 0;
 };
+
+// Stack entries per warp of the group and per-body walks: 48 per tree level
+// plus 32 (a step pops 16 entries and pushes at most 32), set per launch
+// from the tree depth; the deepest group-walk stack of every launch is
+// recorded in counters[2].
+constexpr int kGWStackPerLevel = 48;
+inline int group_stack_cap(int levels) { return kGWStackPerLevel * (levels + 1) + 32; }
 
 constexpr int kPartTile = 2048;  // elements per partition tile (256 threads x 8)
 
@@ -112,6 +127,9 @@ nbg_status tree_refit(nbg_engine* e, const double* y, double lambda);
 nbg_status bh_tree(nbg_engine* e, uint64_t step, const double* y, bool fp64_nodes, double lambda);
 // The plain mixed-precision walk over the current tree (group walk by
 // default, "bh.walk" = 0 the warp-coherent walk), writing all of f.
-nbg_status mixed_walk(nbg_engine* e, const double* y, double* f);
+// emit: the default group walk also records each group's band cells (the
+// fields cand, cand_n, cand_cap, band2 set) and the per-body fallback walk is
+// left to the caller (f of the groups in fb_list is not written).
+nbg_status mixed_walk(nbg_engine* e, const double* y, double* f, bool emit = false);
 
 }  // namespace nbg

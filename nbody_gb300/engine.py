@@ -537,6 +537,26 @@ class NbodyEngineGB300:
                                                 out.ctypes.data_as(fp)), "learn_predict")
         return out
 
+    def learn_predict_tc(self, x) -> np.ndarray:
+        """The network's outputs from the tcgen05 tensor-core inference."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        out = np.zeros((x.shape[0], 3), dtype=np.float32)
+        fp = C.POINTER(C.c_float)
+        self._check(self._lib.nbg_learn_predict_tc(self._h, x.ctypes.data_as(fp), x.shape[0],
+                                                   out.ctypes.data_as(fp)), "learn_predict_tc")
+        return out
+
+    def learn_tc_accumulators(self, x) -> np.ndarray:
+        """[count, 144]: the tcgen05 forward pass's accumulators, D1 (columns
+        0..63), D2 (64..127) and D3 (128..143), biases not added."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        out = np.zeros((x.shape[0], 144), dtype=np.float32)
+        fp = C.POINTER(C.c_float)
+        self._check(self._lib.nbg_learn_tc_accumulators(self._h, x.ctypes.data_as(fp), x.shape[0],
+                                                        out.ctypes.data_as(fp)),
+                    "learn_tc_accumulators")
+        return out
+
     def learn_judge_stats(self) -> dict:
         """The learned path's judge (nbg_learn_judge_stats): the last judged
         step's p50 / p99 / RMS relative force errors of the learned and the

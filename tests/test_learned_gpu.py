@@ -162,6 +162,137 @@ def test_inference_path_matches_fp64_forward(make_engine, trained):
     assert np.linalg.norm(got - ref) <= 3e-2 * np.linalg.norm(ref)
 
 
+# ---------------------------------------------------------------------------
+# inference on the tcgen05 tensor cores ("learned.walk" = 1, the default)
+# ---------------------------------------------------------------------------
+def _random_weights(seed, scale=0.3):
+    return np.random.default_rng(seed).normal(0, scale, M.N_PARAMS).astype(np.float32)
+
+
+def _features(count, seed):
+    x = np.random.default_rng(seed).normal(0, 0.7, size=(count, 16)).astype(np.float32)
+    x[:, 12] = np.abs(x[:, 12])
+    return x
+
+
+def test_tensor_core_layouts(make_engine):
+    """The tcgen05 operand, instruction-descriptor and tensor-memory layouts,
+    layer by layer, on random weights with nonzero biases: the accumulators
+    D1 = X W1, D2 = GELU(D1 + b1) W2 and D3 = GELU(D2 + b2) W3 (columns
+    past 3 zero).  D1 is a sum of 16 exact BF16 products in FP32; the next
+    layers are checked from the GPU's own previous accumulators (whose GELU
+    rounds to BF16 the same way)."""
+    e = _bh_engine(make_engine, 1.0 / 0.9, learned=True)
+    assert e.init(NBodyData.plummer(1024, seed=1))
+    w = _random_weights(3)
+    e.learn_set_weights(w)
+    W1, _, W2, _, W3, _ = M.unpack(M.bf16(w))
+    b1, b2 = M.unpack(w)[1], M.unpack(w)[3]  # biases stay FP32
+    for count in (1, 200, 4096):
+        x = _features(count, 11 + count)
+        acc = e.learn_tc_accumulators(x).astype(np.float64)
+        d1, d2, d3 = acc[:, 0:64], acc[:, 64:128], acc[:, 128:144]
+        xb = M.bf16(x)
+        err1 = np.abs(d1 - xb @ W1) / (np.abs(xb) @ np.abs(W1) + 1e-30)
+        z2 = M.bf16(M.gelu(d1 + b1)) @ W2
+        err2 = np.linalg.norm(d2 - z2) / np.linalg.norm(z2)
+        z3 = M.bf16(M.gelu(d2 + b2)) @ W3
+        err3 = np.linalg.norm(d3[:, :3] - z3) / np.linalg.norm(z3)
+        print(f"\ncount {count}: D1 max err / bound {err1.max():.2e}, D2 rel err {err2:.2e}, "
+              f"D3 rel err {err3:.2e}")
+        assert err1.max() < 1e-5
+        assert err2 < 1e-2
+        assert err3 < 1e-2
+        assert np.all(d3[:, 3:] == 0.0)
+
+
+@pytest.mark.parametrize("count", [1, 127, 128, 1000, 70001])
+def test_tensor_core_inference_matches_mma_sync(make_engine, count):
+    """The tcgen05 inference against the walk's mma.sync routine and the FP64
+    forward pass on the same BF16 weights and inputs, for counts that are
+    and are not multiples of the 128-row tile.  Both round the activations
+    to BF16; their FP32 sums run in different orders, so an activation can
+    round to the neighbouring BF16 value."""
+    e = _bh_engine(make_engine, 1.0 / 0.9, learned=True)
+    assert e.init(NBodyData.plummer(1024, seed=1))
+    w = _random_weights(4)
+    e.learn_set_weights(w)
+    x = _features(count, 5 + count)
+    tc = e.learn_predict_tc(x).astype(np.float64)
+    ms = e.learn_predict(x).astype(np.float64)
+    ref = M.forward(M.bf16(w), M.bf16(x))
+    assert np.all(np.isfinite(tc))
+    d_ms = np.linalg.norm(tc - ms) / np.linalg.norm(ms)
+    d_ref = np.linalg.norm(tc - ref) / np.linalg.norm(ref)
+    print(f"\ncount {count}: |tc - mma.sync| / |mma.sync| {d_ms:.2e}, "
+          f"|tc - fp64| / |fp64| {d_ref:.2e}")
+    assert d_ms < 1e-2
+    assert d_ref < 3e-2
+
+
+def test_tensor_core_walk_with_zero_network_is_the_group_walk(make_engine):
+    """Zero weights make every correction exactly zero, so the tensor-core
+    learned walk equals the plain group walk at the loose ratio on the same
+    tree (FP64 nodes) bit for bit -- with the group walk's band-cell records
+    in place, and with every group handed to the per-body learned walk
+    (bh.test_cap = 1)."""
+    n = 1 << 15
+    d = NBodyData.plummer(n, seed=41)
+    for cap in (0, 1):
+        plain = _bh_engine(make_engine, 1.0 / 0.9)
+        plain.tune_set("bh.fp64_nodes", 1)
+        plain.tune_set("bh.test_cap", cap)
+        assert plain.init(d)
+        f_plain = _forces(plain, n)
+        e = _bh_engine(make_engine, 1.0 / 0.9, learned=True)
+        e.tune_set("learned.judge", 0)
+        e.tune_set("bh.test_cap", cap)
+        assert e.init(d)
+        e.learn_set_weights(np.zeros(M.N_PARAMS, dtype=np.float32))
+        f = _forces(e, n)
+        rows = e.learn_band_rows()
+        print(f"\ntest_cap {cap}: band rows per body {rows / n:.1f}")
+        assert rows > 0
+        assert np.array_equal(f, f_plain)
+
+
+def test_tensor_core_walk_vs_plain(make_engine, oracle, trained):
+    """The trained network on the tensor-core group walk at theta = 0.9,
+    judged by the FP64 direct sum on a snapshot the network never saw: lower
+    median and p99 than the plain group walk at theta = 0.9 on the same tree;
+    equal inputs give equal forces (the per-body sums run in a fixed
+    order)."""
+    w = trained[0]
+    n = 1 << 15
+    d = NBodyData.plummer(n, seed=77)
+    y = d.to_state()
+    rows = np.random.default_rng(4).choice(n, size=512, replace=False)
+    a_ref = oracle.accel_rows(y, d.mass, EPS, rows=rows)
+
+    def rel(out):
+        a = out[3 * n:].reshape(3, n).T[rows]
+        return np.linalg.norm(a - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
+
+    plain = _bh_engine(make_engine, 1.0 / 0.9)
+    plain.tune_set("bh.fp64_nodes", 1)
+    assert plain.init(d)
+    r_plain = rel(_forces(plain, n))
+    e = _bh_engine(make_engine, 1.0 / 0.9, learned=True)
+    e.tune_set("learned.judge", 0)
+    assert e.init(d)
+    e.learn_set_weights(w)
+    f1 = _forces(e, n)
+    f2 = _forces(e, n)
+    assert np.all(np.isfinite(f1))
+    assert np.array_equal(f1, f2)
+    assert np.array_equal(f1[:3 * n], y[3 * n:])
+    r = rel(f1)
+    q = lambda v: f"p50 {np.median(v):.3e} p99 {np.quantile(v, 0.99):.3e}"
+    print(f"\ngroup walk theta0.9: plain {q(r_plain)} | learned (tcgen05) {q(r)}")
+    assert np.median(r) < 0.95 * np.median(r_plain)
+    assert np.quantile(r, 0.99) < np.quantile(r_plain, 0.99)
+
+
 @pytest.mark.parametrize("group", [0, 1])
 def test_learned_walk_vs_plain(make_engine, oracle, trained, group):
     """What the trained network changes in the force at theta = 0.9, judged by
@@ -277,7 +408,7 @@ def test_judge_trips_on_bad_weights_and_falls_back_bit_for_bit(make_engine):
 
 def test_judge_figures_and_decision(make_engine, oracle):
     """With a correction that changes nothing (zero weights) the learned walk
-    is the warp-coherent walk at the loose ratio.  The judge's learned p50
+    is the group walk at the loose ratio.  The judge's learned p50
     and p99 equal a host recomputation on the same sampled bodies (the
     learned walk's forces against the FP64 direct sum); its plain figures
     equal the per-body walk at the tight ratio (the group walk forced to its
