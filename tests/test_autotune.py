@@ -111,7 +111,7 @@ def test_engine_autotune_bh(make_engine):
     assert keys[6:8] == [dict(g64, **{"bh.walk_blocks": 4, "bh.acc_smem": 0, "bh.eval_unroll": u})
                          for u in (1, 4)]
     assert keys[8:] == [{"bh.walk": 1, "bh.group": 32, "bh.walk_blocks": b} for b in (6, 8)] + \
-        [{"bh.walk": 0}]
+        [{"bh.walk": 1, "bh.group": 128}, {"bh.walk": 0}]
     assert e.tune_get("bh.walk") == rep["best"]["bh.walk"]
 
 
