@@ -28,6 +28,7 @@ to --suites-out (default bench_out/suites.json):
   ensemble    2048 Plummer clusters stepped by the device-side rkdp;
   statistics  P, L, E, V of one state on the GPU against the host sums.
     python bench.py --bh-only [--bh-n N] [--bh-cases a,b]   the suite alone
+    python bench.py --ensemble-only [--steps K]              the ensemble alone
 """
 from __future__ import annotations
 
@@ -63,6 +64,8 @@ def parse():
     ap.add_argument("--n", type=int, default=N_BODIES)
     ap.add_argument("--no-bh", action="store_true", help="skip the Barnes-Hut measurements")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble measurements")
+    ap.add_argument("--ensemble-only", action="store_true",
+                    help="run only the ensemble measurement (config 5); prints its JSON")
     ap.add_argument("--bh-only", action="store_true",
                     help="run only the Barnes-Hut suite (with --bh-n bodies); prints its JSON")
     ap.add_argument("--bh-n", type=int, default=1 << 20, help="bodies of the Barnes-Hut suite")
@@ -949,6 +952,9 @@ def main():
     if args.bh_only:
         cases = [c for c in args.bh_cases.split(",") if c] or None
         print(json.dumps(run_bh_suite(0, args.bh_n, cases, args.bh_train_samples)), flush=True)
+        return
+    if args.ensemble_only:
+        print(json.dumps(run_ensemble_suite(steps=args.steps)), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

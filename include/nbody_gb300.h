@@ -396,8 +396,12 @@ nbg_status nbg_ensemble_fcompute(nbg_ensemble* s, double* f);
 /* 12 FP64 conservation sums per system (layout of nbg_statistics, softened
  * potential of the ensemble's softening). */
 nbg_status nbg_ensemble_statistics(nbg_ensemble* s, double* out);
-/* Tuning keys "ensemble.pairs_per_lane" (1 or 2: i-tile of 256 or 512 bodies
- * per work unit), "ensemble.blocks_per_sm" (0 = as many as fit),
+/* Tuning keys "ensemble.symmetric" (1, the default: every unordered pair of
+ * a system evaluated once for both bodies, the reaction sums kept as
+ * per-range partials and added in a fixed order, so results stay
+ * bit-reproducible; 0: the one-sided kernel), "ensemble.pairs_per_lane" (1
+ * or 2: i-tile of 256 or 512 bodies per work unit), "ensemble.blocks_per_sm"
+ * (0 = as many as fit),
  * "ensemble.unroll" (2, 4 or 8: j-loop unroll of the force kernel),
  * "ensemble.uniform_mass" (1, the default: when every system has equal
  * masses, pairs are weighted by r^-3 alone and each system's mass scales its

@@ -28,6 +28,7 @@
 #include <mutex>
 
 #include "nbg_internal.cuh"
+#include "nbg_pair.cuh"
 #include "nbg_ptx.cuh"
 
 namespace nbg {
@@ -417,63 +418,6 @@ struct SymCursor {
         }
     }
 };
-
-template <bool CLAMP>
-__device__ __forceinline__ void sym_pair(f2_t xj, f2_t yj, f2_t zj, f2_t mj, f2_t xi, f2_t yi,
-                                         f2_t zi, f2_t mi, f2_t eps2, f2_t& ax, f2_t& ay,
-                                         f2_t& az, f2_t& bx, f2_t& by, f2_t& bz) {
-    const f2_t dx = f2_sub(xj, xi);
-    const f2_t dy = f2_sub(yj, yi);
-    const f2_t dz = f2_sub(zj, zi);
-    f2_t r2 = f2_fma(dz, dz, eps2);
-    r2 = f2_fma(dy, dy, r2);
-    r2 = f2_fma(dx, dx, r2);
-    float r2a, r2b;
-    f2_unpack(r2, r2a, r2b);
-    if (CLAMP) {
-        r2a = fmaxf(r2a, 1e-8f);
-        r2b = fmaxf(r2b, 1e-8f);
-    }
-    const f2_t inv = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
-    const f2_t inv3 = f2_mul(f2_mul(inv, inv), inv);
-    const f2_t sa = f2_mul(mj, inv3);
-    const f2_t sb = f2_mul(mi, inv3);
-    ax = f2_fma(dx, sa, ax);
-    ay = f2_fma(dy, sa, ay);
-    az = f2_fma(dz, sa, az);
-    bx = f2_fma(dx, sb, bx);
-    by = f2_fma(dy, sb, by);
-    bz = f2_fma(dz, sb, bz);
-}
-
-// Equal masses: the pair weights reduce to r^-3 and the common mass scales
-// the sums once, in FP64, when they are added to f (14 packed operations per
-// pair evaluation instead of 16; 1 fewer for a one-sided pair).
-template <bool CLAMP>
-__device__ __forceinline__ void sym_pair_uni(f2_t xj, f2_t yj, f2_t zj, f2_t xi, f2_t yi,
-                                             f2_t zi, f2_t eps2, f2_t& ax, f2_t& ay, f2_t& az,
-                                             f2_t& bx, f2_t& by, f2_t& bz) {
-    const f2_t dx = f2_sub(xj, xi);
-    const f2_t dy = f2_sub(yj, yi);
-    const f2_t dz = f2_sub(zj, zi);
-    f2_t r2 = f2_fma(dz, dz, eps2);
-    r2 = f2_fma(dy, dy, r2);
-    r2 = f2_fma(dx, dx, r2);
-    float r2a, r2b;
-    f2_unpack(r2, r2a, r2b);
-    if (CLAMP) {
-        r2a = fmaxf(r2a, 1e-8f);
-        r2b = fmaxf(r2b, 1e-8f);
-    }
-    const f2_t inv = f2_pack(rsqrt_mufu(r2a), rsqrt_mufu(r2b));
-    const f2_t inv3 = f2_mul(f2_mul(inv, inv), inv);
-    ax = f2_fma(dx, inv3, ax);
-    ay = f2_fma(dy, inv3, ay);
-    az = f2_fma(dz, inv3, az);
-    bx = f2_fma(dx, inv3, bx);
-    by = f2_fma(dy, inv3, by);
-    bz = f2_fma(dz, inv3, bz);
-}
 
 template <bool CLAMP>
 __device__ __forceinline__ void pair_uni(f2_t xj, f2_t yj, f2_t zj, f2_t xi, f2_t yi, f2_t zi,

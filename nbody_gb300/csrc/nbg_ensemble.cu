@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "nbg_internal.cuh"
+#include "nbg_pair.cuh"
 #include "nbg_ptx.cuh"
 #include "nbg_stats.cuh"
 #include "nbg_tune.cuh"
@@ -243,6 +244,227 @@ ens_force_kernel(const Body2* __restrict__ bodies, const long long* __restrict__
     }
 }
 
+// ---------------------------------------------------------------------------
+// symmetric force kernel: every unordered pair of a system evaluated once
+// ---------------------------------------------------------------------------
+// A system's bodies split into A ranges of 256 G (G packed pairs per lane)
+// and B tiles of 128.  Unit (s, R) holds range R's bodies in registers and
+// walks the tiles from R's first on:
+//   * R's own tiles: one-sided, all ordered pairs, A side only;
+//   * every later tile: symmetric (nbg_pair.cuh).  The B bodies of a
+//     32-body chunk rotate through each warp -- at step r lane l meets chunk
+//     body (l + r) mod 32, and the body's FP32 sum follows it one lane down
+//     per step -- the four warps' sums are added in warp order, and the unit
+//     writes one FP32 partial per (R, B body) to bpart.
+// Tiles before R are covered by the units of their own ranges.  The A sums
+// (two-sum per tile) go straight to the output; ens_sym_reduce_kernel then
+// adds to every body the partials of the ranges before its own, in range
+// order, in FP64 (weight -1, or -m with equal masses).  No atomics: equal
+// states give equal forces.  Per pair of bodies 14 to 16 packed FP32
+// operations and one reciprocal square root serve both bodies, against 11
+// to 12 operations per body and pair in the one-sided kernel.
+struct EnsSymUnit {
+    int sys;
+    int r;  // A range
+};
+
+// at least 4 CTAs per SM: a 128-register budget, which the 4-body (G = 2)
+// equal-mass build needs to run without spills
+template <bool CLAMP, int G, bool UNI>
+__global__ void __launch_bounds__(kEnsThreads, 4)
+ens_sym_kernel(const Body2* __restrict__ bodies, const long long* __restrict__ off,
+               const int* __restrict__ cnt, const EnsSymUnit* __restrict__ units, int nunits,
+               unsigned* __restrict__ counter, double* __restrict__ acc, size_t B, float eps2v,
+               const double* __restrict__ sys_mass, float* __restrict__ bpart,
+               const long long* __restrict__ boff, size_t bstride) {
+    constexpr int RA = kEnsThreads * 2 * G;
+    constexpr int TPR = RA / kEnsTile;
+    __shared__ __align__(16) float4 txy[kEnsTile];  // (x x y y) per body
+    __shared__ __align__(16) float4 tzm[kEnsTile];  // (z z m m) per body
+    __shared__ float bsum[kEnsThreads / 32][3][kEnsTile];
+    __shared__ int next_unit;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const f2_t eps2 = f2_pack(eps2v, eps2v);
+    const f2_t zero = f2_pack(0.f, 0.f);
+    const uint32_t xy_addr = smem_addr(txy), zm_addr = smem_addr(tzm);
+    // stand-in for the slots past a system's end: far away and massless, so
+    // its r^-3 underflows to zero against every real body
+    const float4 far_xy = make_float4(1e18f, 1e18f, 1e18f, 1e18f);
+    const float4 far_zm = make_float4(1e18f, 1e18f, 0.f, 0.f);
+    while (true) {
+        __syncthreads();
+        if (threadIdx.x == 0) next_unit = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int u = next_unit;
+        if (u >= nunits) break;
+        const EnsSymUnit un = units[u];
+        const long long o = off[un.sys];
+        const int n = cnt[un.sys];
+        const int a0 = un.r * RA;
+        const int tiles = (n + kEnsTile - 1) / kEnsTile;
+        f2_t xi[G], yi[G], zi[G], mi[G], hx[G], hy[G], hz[G], lx[G], ly[G], lz[G];
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            const int l0 = a0 + (2 * g) * kEnsThreads + threadIdx.x;
+            const int l1 = l0 + kEnsThreads;
+            float4 p0 = far_xy, q0 = far_zm, p1 = far_xy, q1 = far_zm;
+            if (l0 < n) {
+                const Body2 b = bodies[o + l0];
+                p0 = b.xxyy;
+                q0 = b.zzmm;
+            }
+            if (l1 < n) {
+                const Body2 b = bodies[o + l1];
+                p1 = b.xxyy;
+                q1 = b.zzmm;
+            }
+            xi[g] = f2_pack(p0.x, p1.x);
+            yi[g] = f2_pack(p0.z, p1.z);
+            zi[g] = f2_pack(q0.x, q1.x);
+            mi[g] = f2_pack(q0.z, q1.z);
+            hx[g] = hy[g] = hz[g] = lx[g] = ly[g] = lz[g] = zero;
+        }
+        for (int t = un.r * TPR; t < tiles; ++t) {
+            __syncthreads();  // the previous tile's readers are done
+            const int j = t * kEnsTile + threadIdx.x;
+            if (j < n) {
+                const Body2 b = bodies[o + j];
+                txy[threadIdx.x] = b.xxyy;
+                tzm[threadIdx.x] = b.zzmm;
+            } else {
+                txy[threadIdx.x] = far_xy;
+                tzm[threadIdx.x] = far_zm;
+            }
+            __syncthreads();
+            f2_t ax[G], ay[G], az[G];
+#pragma unroll
+            for (int g = 0; g < G; ++g) ax[g] = ay[g] = az[g] = zero;
+            const int jn = min(kEnsTile, n - t * kEnsTile);
+            if (t < (un.r + 1) * TPR) {
+                // the range's own tile: one-sided, broadcast loads
+#pragma unroll 4
+                for (int jj = 0; jj < jn; ++jj) {
+                    const float4 p = lds128(xy_addr + 16u * jj);
+                    const float4 q = lds128(zm_addr + 16u * jj);
+                    const f2_t xj = f2_pack(p.x, p.y), yj = f2_pack(p.z, p.w);
+                    const f2_t zj = f2_pack(q.x, q.y), mj = f2_pack(q.z, q.w);
+#pragma unroll
+                    for (int g = 0; g < G; ++g) {
+                        if constexpr (UNI)
+                            pair2e_uni<CLAMP>(xj, yj, zj, xi[g], yi[g], zi[g], eps2, ax[g],
+                                              ay[g], az[g]);
+                        else
+                            pair2e<CLAMP>(xj, yj, zj, mj, xi[g], yi[g], zi[g], eps2, ax[g],
+                                          ay[g], az[g]);
+                    }
+                }
+            } else {
+#pragma unroll 1
+                for (int c = 0; c < kEnsTile / 32; ++c) {
+                    float bx = 0.f, by = 0.f, bz = 0.f;
+                    if (c * 32 < jn) {  // chunks wholly past the end are skipped
+#pragma unroll 8
+                        for (int r = 0; r < 32; ++r) {
+                            const uint32_t idx = (uint32_t)(c * 32 + ((lane + r) & 31));
+                            const float4 p = lds128(xy_addr + 16u * idx);
+                            const float4 q = lds128(zm_addr + 16u * idx);
+                            const f2_t xj = f2_pack(p.x, p.y), yj = f2_pack(p.z, p.w);
+                            const f2_t zj = f2_pack(q.x, q.y), mj = f2_pack(q.z, q.w);
+                            f2_t px = zero, py = zero, pz = zero;
+#pragma unroll
+                            for (int g = 0; g < G; ++g) {
+                                if constexpr (UNI)
+                                    sym_pair_uni<CLAMP>(xj, yj, zj, xi[g], yi[g], zi[g], eps2,
+                                                        ax[g], ay[g], az[g], px, py, pz);
+                                else
+                                    sym_pair<CLAMP>(xj, yj, zj, mj, xi[g], yi[g], zi[g], mi[g],
+                                                    eps2, ax[g], ay[g], az[g], px, py, pz);
+                            }
+                            float lo, hi;
+                            f2_unpack(px, lo, hi);
+                            bx += lo + hi;
+                            f2_unpack(py, lo, hi);
+                            by += lo + hi;
+                            f2_unpack(pz, lo, hi);
+                            bz += lo + hi;
+                            // the sum of chunk body (lane + r) moves to lane - 1,
+                            // which meets that body at step r + 1
+                            const int src = (lane + 1) & 31;
+                            bx = __shfl_sync(0xffffffffu, bx, src);
+                            by = __shfl_sync(0xffffffffu, by, src);
+                            bz = __shfl_sync(0xffffffffu, bz, src);
+                        }
+                    }
+                    // after 32 steps and shifts lane l holds chunk body l's sum
+                    bsum[warp][0][c * 32 + lane] = bx;
+                    bsum[warp][1][c * 32 + lane] = by;
+                    bsum[warp][2][c * 32 + lane] = bz;
+                }
+                __syncthreads();
+                if ((int)threadIdx.x < jn) {
+                    const size_t base = (size_t)boff[un.sys] + (size_t)un.r * n +
+                                        (size_t)t * kEnsTile + threadIdx.x;
+#pragma unroll
+                    for (int comp = 0; comp < 3; ++comp) {
+                        float v = bsum[0][comp][threadIdx.x];
+#pragma unroll
+                        for (int w = 1; w < kEnsThreads / 32; ++w) v += bsum[w][comp][threadIdx.x];
+                        bpart[comp * bstride + base] = v;
+                    }
+                }
+            }
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                f2_two_sum(hx[g], lx[g], ax[g]);
+                f2_two_sum(hy[g], ly[g], ay[g]);
+                f2_two_sum(hz[g], lz[g], az[g]);
+            }
+        }
+        const double w = UNI ? sys_mass[un.sys] : 1.0;
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            const int l0 = a0 + (2 * g) * kEnsThreads + threadIdx.x;
+            const int l1 = l0 + kEnsThreads;
+            const f2_t hh[3] = {hx[g], hy[g], hz[g]};
+            const f2_t ll[3] = {lx[g], ly[g], lz[g]};
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float h0, h1, q0, q1;
+                f2_unpack(hh[c], h0, h1);
+                f2_unpack(ll[c], q0, q1);
+                if (l0 < n) acc[c * B + o + l0] = w * ((double)h0 + (double)q0);
+                if (l1 < n) acc[c * B + o + l1] = w * ((double)h1 + (double)q1);
+            }
+        }
+    }
+}
+
+// Adds to every body the B partials of the ranges before its own, in range
+// order, in FP64: acc += w sum_r bpart[r], w = -1 (or -m with equal masses).
+__global__ void ens_sym_reduce_kernel(const int* __restrict__ sys, const long long* __restrict__ off,
+                                      const int* __restrict__ cnt,
+                                      const float* __restrict__ bpart,
+                                      const long long* __restrict__ boff, size_t bstride,
+                                      double* __restrict__ acc, size_t B,
+                                      const double* __restrict__ sys_mass, int uni, int ra) {
+    for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < B;
+         j += (size_t)gridDim.x * blockDim.x) {
+        const int s = sys[j];
+        const int l = (int)((long long)j - off[s]);
+        const int rj = l / ra;
+        if (rj == 0) continue;
+        const int n = cnt[s];
+        const double w = uni ? -sys_mass[s] : -1.0;
+        const size_t base = (size_t)boff[s] + (size_t)l;
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+            double sum = 0.0;
+            for (int r = 0; r < rj; ++r) sum += (double)bpart[comp * bstride + base + (size_t)r * n];
+            acc[comp * B + j] += w * sum;
+        }
+    }
+}
+
 // Candidate update y_new = y + dt sum b2_i k_i and per-system error
 // max |dt sum (b2_i - b1_i) k_i| (as ordered bits, atomicMax).
 __global__ void ens_error_kernel(const double* __restrict__ y, const int* __restrict__ sys,
@@ -351,6 +573,14 @@ struct nbg_ensemble {
     cudaGraph_t graph_def = nullptr;
     int G = 2;
     unsigned force_grid = 1;
+    // symmetric kernel ("ensemble.symmetric"): its units, the B partials
+    // (3 components x bstride floats; system s from boff[s], ranges x N_s)
+    bool sym = false;
+    EnsSymUnit* sym_units = nullptr;
+    int nsym_units = 0;
+    float* bpart = nullptr;
+    size_t bstride = 0, bpart_cap = 0;
+    long long* boff = nullptr;
 };
 
 namespace {
@@ -383,12 +613,94 @@ EnsForce ens_pick(const nbg_ensemble* s) {
     return ens_uniform(s) ? ens_pick_g<true>(clamp, s->G, u) : ens_pick_g<false>(clamp, s->G, u);
 }
 
+using EnsSym = void (*)(const Body2*, const long long*, const int*, const EnsSymUnit*, int,
+                        unsigned*, double*, size_t, float, const double*, float*,
+                        const long long*, size_t);
+
+template <bool UNI>
+EnsSym ens_pick_sym_g(bool clamp, int G) {
+    return clamp ? (G == 1 ? ens_sym_kernel<true, 1, UNI> : ens_sym_kernel<true, 2, UNI>)
+                 : (G == 1 ? ens_sym_kernel<false, 1, UNI> : ens_sym_kernel<false, 2, UNI>);
+}
+
+EnsSym ens_pick_sym(const nbg_ensemble* s) {
+    const bool clamp = !(s->p.softening > 0.0);
+    return ens_uniform(s) ? ens_pick_sym_g<true>(clamp, s->G) : ens_pick_sym_g<false>(clamp, s->G);
+}
+
+// The symmetric kernel's units, cost-ordered (largest first, so the tail of
+// the persistent launch is made of small units), and its partial buffer.
+nbg_status ens_configure_sym(nbg_ensemble* s) {
+    nbg_engine* e = s->eng;
+    const int ra = kEnsThreads * 2 * s->G;
+    struct Costed {
+        EnsSymUnit u;
+        double cost;
+    };
+    std::vector<Costed> units;
+    std::vector<long long> boff(s->nsys);
+    long long total = 0;
+    for (int sI = 0; sI < s->nsys; ++sI) {
+        const int n = s->h_cnt[sI];
+        const int ranges = (n + ra - 1) / ra;
+        boff[sI] = total;
+        total += (long long)ranges * n;
+        for (int r = 0; r < ranges; ++r) {
+            const double own = (double)ra * std::min(ra, n - r * ra);
+            const double later = (double)ra * std::max(0, n - (r + 1) * ra);
+            units.push_back({EnsSymUnit{sI, r}, own + 0.6 * later});
+        }
+    }
+    std::stable_sort(units.begin(), units.end(),
+                     [](const Costed& a, const Costed& b) { return a.cost > b.cost; });
+    std::vector<EnsSymUnit> list(units.size());
+    for (size_t i = 0; i < units.size(); ++i) list[i] = units[i].u;
+    s->nsym_units = (int)list.size();
+    cudaFree(s->sym_units);
+    cudaFree(s->boff);
+    s->sym_units = nullptr;
+    s->boff = nullptr;
+    NBG_CUDA(e, cudaMalloc(&s->sym_units, list.size() * sizeof(EnsSymUnit)));
+    NBG_CUDA(e, cudaMemcpy(s->sym_units, list.data(), list.size() * sizeof(EnsSymUnit),
+                           cudaMemcpyHostToDevice));
+    NBG_CUDA(e, cudaMalloc(&s->boff, boff.size() * sizeof(long long)));
+    NBG_CUDA(e, cudaMemcpy(s->boff, boff.data(), boff.size() * sizeof(long long),
+                           cudaMemcpyHostToDevice));
+    s->bstride = (size_t)std::max<long long>(total, 1);
+    if (s->bpart_cap < 3 * s->bstride) {
+        cudaFree(s->bpart);
+        s->bpart = nullptr;
+        s->bpart_cap = 0;
+        NBG_CUDA(e, cudaMalloc(&s->bpart, 3 * s->bstride * sizeof(float)));
+        s->bpart_cap = 3 * s->bstride;
+    }
+    int occ = 0;
+    NBG_CUDA(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ens_pick_sym(s), kEnsThreads, 0));
+    occ = std::max(occ, 1);
+    const int64_t bps = e->tune_get("ensemble.blocks_per_sm", 0);
+    if (bps > 0 && bps < occ) occ = (int)bps;
+    s->force_grid = (unsigned)std::max(1, std::min(s->nsym_units, e->sm_count * occ));
+    return NBG_OK;
+}
+
 // Work units and launch shape from the tuning keys (the i-block tile of
-// 256 G bodies, CTAs per SM); drops a captured step graph built for an
-// older shape.
+// 256 G bodies, CTAs per SM; "ensemble.symmetric" 1, the default: every
+// unordered pair once); drops a captured step graph built for an older
+// shape.
 nbg_status ens_configure(nbg_ensemble* s) {
     nbg_engine* e = s->eng;
     s->G = (int)std::max<int64_t>(1, std::min<int64_t>(2, e->tune_get("ensemble.pairs_per_lane", 2)));
+    s->sym = e->tune_get("ensemble.symmetric", 1) != 0;
+    if (s->sym) {
+        NBG_CUDA(e, cudaStreamSynchronize(e->stream));
+        nbg_status st = ens_configure_sym(s);
+        if (st != NBG_OK) return st;
+        if (s->graph) cudaGraphExecDestroy(s->graph);
+        if (s->graph_def) cudaGraphDestroy(s->graph_def);
+        s->graph = nullptr;
+        s->graph_def = nullptr;
+        return NBG_OK;
+    }
     const int blk = kEnsThreads * 2 * s->G;
     std::vector<EnsUnit> units;
     for (int sI = 0; sI < s->nsys; ++sI)
@@ -418,6 +730,29 @@ nbg_status ens_configure(nbg_ensemble* s) {
     return NBG_OK;
 }
 
+// The RHS of one stage: forces of the FP32 body records into acc ([3][B],
+// the acceleration half of a k buffer).
+nbg_status ens_launch_force(nbg_ensemble* s, unsigned* counter, double* acc) {
+    nbg_engine* e = s->eng;
+    const float eps2 = (float)(s->p.softening * s->p.softening);
+    if (s->sym) {
+        ens_pick_sym(s)<<<s->force_grid, kEnsThreads, 0, e->stream>>>(
+            s->bodies, s->off, s->cnt, s->sym_units, s->nsym_units, counter, acc, s->B, eps2,
+            s->sys_mass, s->bpart, s->boff, s->bstride);
+        NBG_LAUNCHED(e, "ens_sym_kernel");
+        ens_sym_reduce_kernel<<<grid_for(s->B, 256, (unsigned)e->sm_count * 8u), 256, 0,
+                                e->stream>>>(s->sys, s->off, s->cnt, s->bpart, s->boff,
+                                             s->bstride, acc, s->B, s->sys_mass,
+                                             ens_uniform(s) ? 1 : 0, kEnsThreads * 2 * s->G);
+        NBG_LAUNCHED(e, "ens_sym_reduce_kernel");
+        return NBG_OK;
+    }
+    ens_pick(s)<<<s->force_grid, kEnsThreads, 0, e->stream>>>(
+        s->bodies, s->off, s->cnt, s->units, s->nunits, counter, acc, s->B, eps2, s->sys_mass);
+    NBG_LAUNCHED(e, "ens_force_kernel");
+    return NBG_OK;
+}
+
 // Stage-0 forces of the current state into k_0 (no host copy).
 nbg_status ens_enqueue_force(nbg_ensemble* s) {
     nbg_engine* e = s->eng;
@@ -428,11 +763,7 @@ nbg_status ens_enqueue_force(nbg_ensemble* s) {
     ens_stage_kernel<<<gv, 256, 0, e->stream>>>(0, s->y, s->mass, s->sys, s->dt, kp, s->B,
                                                 s->bodies);
     NBG_LAUNCHED(e, "ens_stage_kernel");
-    ens_pick(s)<<<s->force_grid, kEnsThreads, 0, e->stream>>>(
-        s->bodies, s->off, s->cnt, s->units, s->nunits, s->counters, s->k[0] + 3 * s->B, s->B,
-        (float)(s->p.softening * s->p.softening), s->sys_mass);
-    NBG_LAUNCHED(e, "ens_force_kernel");
-    return NBG_OK;
+    return ens_launch_force(s, s->counters, s->k[0] + 3 * s->B);
 }
 
 nbg_status ens_enqueue_step(nbg_ensemble* s) {
@@ -442,18 +773,13 @@ nbg_status ens_enqueue_step(nbg_ensemble* s) {
     for (int i = 0; i < kStagesRK; ++i) kp.k[i] = s->k[i];
     NBG_CUDA(e, cudaMemsetAsync(s->counters, 0, kStagesRK * sizeof(unsigned), e->stream));
     NBG_CUDA(e, cudaMemsetAsync(s->err, 0, s->nsys * sizeof(unsigned long long), e->stream));
-    const float eps2 = (float)(s->p.softening * s->p.softening);
-    auto kern = ens_pick(s);
-    const unsigned grid = s->force_grid;
     for (int st = 0; st < kStagesRK; ++st) {
         ens_stage_kernel<<<gv, 256, 0, e->stream>>>(st, s->y, s->mass, s->sys, s->dt, kp, s->B,
                                                     s->bodies);
         NBG_LAUNCHED(e, "ens_stage_kernel");
         ProfScope ps(e, NBG_K_DIRECT);
-        kern<<<grid, kEnsThreads, 0, e->stream>>>(s->bodies, s->off, s->cnt, s->units, s->nunits,
-                                                  s->counters + st, s->k[st] + 3 * s->B, s->B, eps2,
-                                                  s->sys_mass);
-        NBG_LAUNCHED(e, "ens_force_kernel");
+        nbg_status fs = ens_launch_force(s, s->counters + st, s->k[st] + 3 * s->B);
+        if (fs != NBG_OK) return fs;
     }
     ens_error_kernel<<<gv, 256, 0, e->stream>>>(s->y, s->sys, s->dt, kp, s->B, s->ynew, s->err);
     NBG_LAUNCHED(e, "ens_error_kernel");
@@ -470,8 +796,12 @@ nbg_status ens_enqueue_step(nbg_ensemble* s) {
 void ens_free(nbg_ensemble* s) {
     void* ptrs[] = {s->off, s->cnt, s->sys, s->y, s->ynew, s->mass, s->sys_mass, s->bodies, s->dt, s->t,
                     s->err, s->accepted, s->rejected, s->decision, s->err_prev, s->units,
-                    s->counters};
+                    s->counters, s->sym_units, s->bpart, s->boff};
     for (void* p : ptrs) cudaFree(p);
+    s->sym_units = nullptr;
+    s->bpart = nullptr;
+    s->boff = nullptr;
+    s->bpart_cap = 0;
     for (double* k : s->k) cudaFree(k);
     if (s->graph) cudaGraphExecDestroy(s->graph);
     if (s->graph_def) cudaGraphDestroy(s->graph_def);
@@ -731,13 +1061,17 @@ nbg_status nbg_ensemble_autotune(nbg_ensemble* s, int reps, char* report, size_t
     NBG_CUDA(e, cudaSetDevice(e->device));
     const std::map<std::string, int64_t> base = e->tune;
     std::vector<Candidate> cands;
-    for (int g : {2, 1})
+    for (int g : {1, 2})  // the symmetric kernel
+        cands.push_back({{{"ensemble.symmetric", 1}, {"ensemble.pairs_per_lane", g},
+                          {"ensemble.blocks_per_sm", 0}}});
+    for (int g : {2, 1})  // the one-sided kernel
         for (int bps : {0, 4, 2})
-            cands.push_back({{{"ensemble.pairs_per_lane", g}, {"ensemble.blocks_per_sm", bps}}});
+            cands.push_back({{{"ensemble.symmetric", 0}, {"ensemble.pairs_per_lane", g},
+                              {"ensemble.blocks_per_sm", bps}}});
     for (int g : {2, 1})
         for (int u : {2, 8})
-            cands.push_back({{{"ensemble.pairs_per_lane", g}, {"ensemble.blocks_per_sm", 0},
-                              {"ensemble.unroll", u}}});
+            cands.push_back({{{"ensemble.symmetric", 0}, {"ensemble.pairs_per_lane", g},
+                              {"ensemble.blocks_per_sm", 0}, {"ensemble.unroll", u}}});
     std::vector<double> ms;
     for (const Candidate& c : cands) {
         e->tune = base;

@@ -153,7 +153,10 @@ def test_ensemble_autotune_keeps_results():
     ens.init(systems)
     f0 = ens.fcompute()
     rep = ens.autotune(2)
-    assert len(rep["candidates"]) == 10 and rep["best"] in [c["keys"] for c in rep["candidates"]]
+    keys = [c["keys"] for c in rep["candidates"]]
+    assert len(keys) == 12 and rep["best"] in keys
+    # the symmetric kernel (G = 1, 2) first, then the one-sided shapes
+    assert [k["ensemble.symmetric"] for k in keys] == [1, 1] + [0] * 10
     f1 = ens.fcompute()
     # another tile shape sums in another order: FP32 rounding only
     scale = np.abs(f0).max()

@@ -149,6 +149,47 @@ def test_ensemble_statistics_unsoftened_match_oracle(gpulib, oracle):
     ens.close()
 
 
+@pytest.mark.parametrize("kind,eps", [("plummer", 1e-3), ("cube", 1e-3), ("plummer", 0.0)],
+                         ids=["equal-mass", "unequal-mass", "clamp"])
+@pytest.mark.parametrize("g", [1, 2])
+def test_symmetric_kernel_matches_one_sided(gpulib, oracle, g, kind, eps):
+    """The symmetric kernel (every unordered pair of a system once; the B
+    sums through per-range FP32 partials and a fixed-order FP64 reduce)
+    against the one-sided kernel on the same systems, sizes around the
+    256 G-body ranges: FP32 rounding apart, both within the oracle's bound,
+    and two evaluations equal bit for bit."""
+    sizes = [1, 33, 255, 256, 257, 513, 700, 4096]
+    sy = _systems(sizes, seed=12, kind=kind)
+    out = {}
+    for sym in (1, 0):
+        ens = Ensemble(softening=eps)
+        ens.tune_set("ensemble.symmetric", sym)
+        ens.tune_set("ensemble.pairs_per_lane", g)
+        ens.init(sy)
+        out[sym] = ens.fcompute()
+        if sym:
+            assert np.array_equal(out[sym], ens.fcompute())
+        ens.close()
+    B = sum(sizes)
+    assert np.array_equal(out[1][:3 * B], out[0][:3 * B])
+    a_s, a_o = (out[k][3 * B:].reshape(3, B).T for k in (1, 0))
+    off = 0
+    for d in sy:
+        n = d.get_count()
+        if n == 1:
+            assert np.all(a_s[off] == 0.0)
+        else:
+            ref = oracle.accel_rows(d.to_state(), d.mass, eps)
+            nr = np.linalg.norm(ref, axis=1)
+            rel_so = np.linalg.norm(a_s[off:off + n] - a_o[off:off + n], axis=1) / nr
+            rel_s = np.linalg.norm(a_s[off:off + n] - ref, axis=1) / nr
+            print(f"n={n} g={g} {kind} eps={eps}: sym vs one-sided rms {np.sqrt(np.mean(rel_so ** 2)):.2e}, "
+                  f"sym vs oracle rms {np.sqrt(np.mean(rel_s ** 2)):.2e}")
+            assert np.sqrt(np.mean(rel_so ** 2)) < 1e-6
+            assert np.sqrt(np.mean(rel_s ** 2)) < 1e-5
+        off += n
+
+
 def test_ensemble_uniform_mass_kernel(gpulib, oracle):
     """Equal masses in every system select the kernel that scales each
     system's sums by its mass once; it agrees with the mass-weighted kernel to
