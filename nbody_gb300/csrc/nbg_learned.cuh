@@ -14,9 +14,9 @@ namespace nbg {
 // Band cells a 64-body group may record for the tensor-core path; a group
 // with more is walked body by body instead.
 constexpr int kCandCap = 2048;
-// tcgen05 operand block: W1^T (64 x 16), W2^T (64 x 64), W3^T (16 x 64, rows
-// past 3 zero) as K-major BF16 core matrices, then the biases b1[64],
-// b2[64], b3[16] (FP32, past 3 zero).
+// tcgen05 operand block: W1^T (64 x 16), W2^T / 2 (64 x 64), W3^T / 2
+// (16 x 64, rows past 3 zero) as K-major BF16 core matrices, then the
+// biases b1[64], b2[64], b3[16] (FP32, past 3 zero).
 constexpr int kTcwW1 = 0;                  // words
 constexpr int kTcwW2 = kTcwW1 + 64 * 16 / 2;
 constexpr int kTcwW3 = kTcwW2 + 64 * 64 / 2;

@@ -81,7 +81,9 @@ size_t tc_smem_bytes() { return std::max(sizeof(TcSmem), kTcSmemFloor); }
 // ---------------------------------------------------------------------------
 // operands from the FP32 master weights
 // ---------------------------------------------------------------------------
-// One thread per BF16 pair (k, k + 1) of one operand row n.
+// One thread per BF16 pair (k, k + 1) of one operand row n.  W2 and W3
+// carry GELU's factor 1/2 (exact in BF16): the epilogue forms 2 GELU(z) =
+// z + z tanh(u) with one FMA, and the products are the same bit for bit.
 __global__ void make_tc_weights_kernel(const float* __restrict__ w, uint32_t* __restrict__ tcw) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     constexpr int q1 = 64 * 8, q2 = q1 + 64 * 32, q3 = q2 + 16 * 32;
@@ -92,11 +94,11 @@ __global__ void make_tc_weights_kernel(const float* __restrict__ w, uint32_t* __
     } else if (q < q2) {  // W2^T: n < 64, K = 64
         const int r = q - q1, n = r / 32, k = 2 * (r % 32);
         tcw[kTcwW2 + tc::kmajor_offset(n, k, 64) / 4] =
-            pack_bf16(w[kOffW2 + k * kH + n], w[kOffW2 + (k + 1) * kH + n]);
+            pack_bf16(0.5f * w[kOffW2 + k * kH + n], 0.5f * w[kOffW2 + (k + 1) * kH + n]);
     } else if (q < q3) {  // W3^T: n < 16 (rows past 3 zero), K = 64
         const int r = q - q2, n = r / 32, k = 2 * (r % 32);
-        const float lo = n < kOut ? w[kOffW3 + k * kOut + n] : 0.f;
-        const float hi = n < kOut ? w[kOffW3 + (k + 1) * kOut + n] : 0.f;
+        const float lo = n < kOut ? 0.5f * w[kOffW3 + k * kOut + n] : 0.f;
+        const float hi = n < kOut ? 0.5f * w[kOffW3 + (k + 1) * kOut + n] : 0.f;
         tcw[kTcwW3 + tc::kmajor_offset(n, k, 64) / 4] = pack_bf16(lo, hi);
     } else if (q < q3 + 144) {  // biases b1[64], b2[64], b3[16]
         const int i = q - q3;
@@ -111,19 +113,19 @@ __global__ void make_tc_weights_kernel(const float* __restrict__ w, uint32_t* __
 // ---------------------------------------------------------------------------
 // one 128-row tile through the network
 // ---------------------------------------------------------------------------
-// GELU of two pre-activations z = acc + bias, packed FP32x2, as BF16x2:
-// 0.5 z (1 + tanh(z (c0 + c1 z^2))), c0 = sqrt(2/pi), c1 = 0.044715 c0 (the
-// tanh form of nbg_mlp.cuh with the cubic factored), MUFU tanh.approx.f32.
+// Twice the GELU of two pre-activations z = acc + bias, packed FP32x2, as
+// BF16x2: z (1 + tanh(z (c0 + c1 z^2))), c0 = sqrt(2/pi), c1 = 0.044715 c0
+// (the tanh form of nbg_mlp.cuh with the cubic factored), MUFU
+// tanh.approx.f32; the next layer's weights carry the factor 1/2.
 __device__ __forceinline__ uint32_t gelu2_bf16(f2_t acc, f2_t bias) {
     constexpr float c0 = kGeluC, c1 = kGeluC * kGeluA;
     const f2_t z = f2_add(acc, bias);
     const f2_t u = f2_mul(z, f2_fma(f2_pack(c1, c1), f2_mul(z, z), f2_pack(c0, c0)));
-    const f2_t h = f2_mul(f2_pack(0.5f, 0.5f), z);
     float ua, ub;
     f2_unpack(u, ua, ub);
     const f2_t t = f2_pack(tanh_mufu(ua), tanh_mufu(ub));
     float ga, gb;
-    f2_unpack(f2_fma(h, t, h), ga, gb);
+    f2_unpack(f2_fma(z, t, z), ga, gb);
     return pack_bf16(ga, gb);
 }
 
