@@ -32,6 +32,7 @@
 #include "nbg_learned.cuh"
 #include "nbg_mlp.cuh"
 #include "nbg_ptx.cuh"
+#include "nbg_stats.cuh"
 #include "nbg_tree.cuh"
 
 namespace nbg {
@@ -969,8 +970,9 @@ nbg_status nbg_learn_generate(nbg_engine* e, size_t max_samples, uint64_t seed,
         std::swap(leaves[i], leaves[j]);
     }
     const int nb = std::min(n, (int)std::max<size_t>(256, max_samples / 64));
-    int* d_bodies = nullptr;
-    NBG_CUDA(e, cudaMalloc(&d_bodies, nb * sizeof(int)));
+    DevScratch s_bodies;  // freed on every return
+    NBG_CUDA(e, cudaMalloc(&s_bodies.p, nb * sizeof(int)));
+    int* d_bodies = s_bodies.as<int>();
     NBG_CUDA(e, cudaMemcpyAsync(d_bodies, leaves.data(), nb * sizeof(int), cudaMemcpyHostToDevice,
                                 e->stream));
     const double lam_l = e->params.distance_to_node_radius_ratio;
@@ -983,7 +985,6 @@ nbg_status nbg_learn_generate(nbg_engine* e, size_t max_samples, uint64_t seed,
     unsigned long long got = 0;
     NBG_CUDA(e, cudaMemcpyAsync(&got, L->pair_count, sizeof(got), cudaMemcpyDeviceToHost, e->stream));
     NBG_CUDA(e, cudaStreamSynchronize(e->stream));
-    cudaFree(d_bodies);
     const size_t np = std::min((size_t)got, max_samples);
     if (np > 0) {
         const double eps2 = e->params.softening * e->params.softening;
@@ -1097,8 +1098,9 @@ nbg_status nbg_learn_train(nbg_engine* e, int epochs, size_t batch, double lr, u
         }
         wnorm = sw > 0.0 ? (float)((double)ntrain / sw) : 0.f;
     }
-    int* d_perm = nullptr;
-    NBG_CUDA(e, cudaMalloc(&d_perm, total * sizeof(int)));
+    DevScratch s_perm;  // freed on every return
+    NBG_CUDA(e, cudaMalloc(&s_perm.p, total * sizeof(int)));
+    int* d_perm = s_perm.as<int>();
     NBG_CUDA(e, cudaMemcpyAsync(d_perm, perm.data(), total * sizeof(int), cudaMemcpyHostToDevice,
                                 e->stream));
     const int adam_threads = 256;
@@ -1142,7 +1144,6 @@ nbg_status nbg_learn_train(nbg_engine* e, int epochs, size_t batch, double lr, u
         NBG_CUDA(e, cudaStreamSynchronize(e->stream));
         val = h[0] / (double)(nval * kOut);
     }
-    cudaFree(d_perm);
     if (train_mse) *train_mse = last_train;
     if (val_mse) *val_mse = val;
     return NBG_OK;
@@ -1153,11 +1154,13 @@ nbg_status nbg_learn_loss_grad(nbg_engine* e, const float* x, const float* t, si
     if (e == nullptr || x == nullptr || t == nullptr || count == 0) return NBG_ERR_INVALID_ARG;
     LearnState* L = e->learn;
     if (L == nullptr || !L->has_weights) return set_error(e, NBG_ERR_NOT_INITIALIZED, "no weights");
-    float *dx = nullptr, *dt = nullptr;
-    int* dord = nullptr;
-    NBG_CUDA(e, cudaMalloc(&dx, count * 16 * sizeof(float)));
-    NBG_CUDA(e, cudaMalloc(&dt, count * 4 * sizeof(float)));
-    NBG_CUDA(e, cudaMalloc(&dord, count * sizeof(int)));
+    DevScratch sx, st, sord;  // freed on every return
+    NBG_CUDA(e, cudaMalloc(&sx.p, count * 16 * sizeof(float)));
+    NBG_CUDA(e, cudaMalloc(&st.p, count * 4 * sizeof(float)));
+    NBG_CUDA(e, cudaMalloc(&sord.p, count * sizeof(int)));
+    float* dx = sx.as<float>();
+    float* dt = st.as<float>();
+    int* dord = sord.as<int>();
     std::vector<int> ord(count);
     for (size_t i = 0; i < count; ++i) ord[i] = (int)i;
     NBG_CUDA(e, cudaMemcpyAsync(dx, x, count * 16 * sizeof(float), cudaMemcpyHostToDevice, e->stream));
@@ -1175,9 +1178,6 @@ nbg_status nbg_learn_loss_grad(nbg_engine* e, const float* x, const float* t, si
                                     e->stream));
     NBG_CUDA(e, cudaStreamSynchronize(e->stream));
     NBG_CUDA(e, cudaMemsetAsync(L->grad, 0, kParams * sizeof(float), e->stream));
-    cudaFree(dx);
-    cudaFree(dt);
-    cudaFree(dord);
     if (loss_sum) *loss_sum = h[0];
     return NBG_OK;
 }
@@ -1185,9 +1185,11 @@ nbg_status nbg_learn_loss_grad(nbg_engine* e, const float* x, const float* t, si
 nbg_status nbg_learn_predict(nbg_engine* e, const float* x, size_t count, float* out) {
     if (e == nullptr || x == nullptr || out == nullptr || count == 0) return NBG_ERR_INVALID_ARG;
     if (!learned_ready(e)) return set_error(e, NBG_ERR_NOT_INITIALIZED, "no weights");
-    float *dx = nullptr, *dout = nullptr;
-    NBG_CUDA(e, cudaMalloc(&dx, count * 16 * sizeof(float)));
-    NBG_CUDA(e, cudaMalloc(&dout, count * 4 * sizeof(float)));
+    DevScratch sx, sout;  // freed on every return
+    NBG_CUDA(e, cudaMalloc(&sx.p, count * 16 * sizeof(float)));
+    NBG_CUDA(e, cudaMalloc(&sout.p, count * 4 * sizeof(float)));
+    float* dx = sx.as<float>();
+    float* dout = sout.as<float>();
     NBG_CUDA(e, cudaMemcpyAsync(dx, x, count * 16 * sizeof(float), cudaMemcpyHostToDevice, e->stream));
     const size_t warps = (count + 31) / 32;
     predict_kernel<<<(unsigned)((warps + 3) / 4), 128, 0, e->stream>>>(dx, count, dout, e->learn->frag,
@@ -1199,8 +1201,6 @@ nbg_status nbg_learn_predict(nbg_engine* e, const float* x, size_t count, float*
     NBG_CUDA(e, cudaStreamSynchronize(e->stream));
     for (size_t i = 0; i < count; ++i)
         for (int c = 0; c < 3; ++c) out[i * 3 + c] = tmp[i * 4 + c];
-    cudaFree(dx);
-    cudaFree(dout);
     return NBG_OK;
 }
 

@@ -32,6 +32,7 @@
 #include "nbg_learned.cuh"
 #include "nbg_mlp.cuh"
 #include "nbg_ptx.cuh"
+#include "nbg_stats.cuh"
 #include "nbg_tc.cuh"
 #include "nbg_tree.cuh"
 
@@ -696,10 +697,13 @@ static nbg_status predict_tc(nbg_engine* e, const float* x, size_t count, float*
     if (!learned_ready(e)) return set_error(e, NBG_ERR_NOT_INITIALIZED, "no weights");
     LearnState* L = e->learn;
     if (L->tc_next == nullptr) NBG_CUDA(e, cudaMalloc(&L->tc_next, 2 * sizeof(unsigned)));
-    float *dx = nullptr, *dout = nullptr, *dacc = nullptr;
-    NBG_CUDA(e, cudaMalloc(&dx, count * 16 * sizeof(float)));
-    NBG_CUDA(e, cudaMalloc(&dout, count * 4 * sizeof(float)));
-    if (acc != nullptr) NBG_CUDA(e, cudaMalloc(&dacc, count * kDumpCols * sizeof(float)));
+    DevScratch sx, sout, sacc;  // freed on every return
+    NBG_CUDA(e, cudaMalloc(&sx.p, count * 16 * sizeof(float)));
+    NBG_CUDA(e, cudaMalloc(&sout.p, count * 4 * sizeof(float)));
+    if (acc != nullptr) NBG_CUDA(e, cudaMalloc(&sacc.p, count * kDumpCols * sizeof(float)));
+    float* dx = sx.as<float>();
+    float* dout = sout.as<float>();
+    float* dacc = sacc.as<float>();
     NBG_CUDA(e, cudaMemcpyAsync(dx, x, count * 16 * sizeof(float), cudaMemcpyHostToDevice,
                                 e->stream));
     nbg_status as = tc_kernel_attrs(e, (const void*)predict_tc_kernel);
@@ -720,9 +724,6 @@ static nbg_status predict_tc(nbg_engine* e, const float* x, size_t count, float*
     if (out != nullptr)
         for (size_t i = 0; i < count; ++i)
             for (int c = 0; c < 3; ++c) out[i * 3 + c] = tmp[i * 4 + c];
-    cudaFree(dx);
-    cudaFree(dout);
-    cudaFree(dacc);
     return NBG_OK;
 }
 
