@@ -678,6 +678,9 @@ def bh_summary(bh):
               "learned_walk_theta_0.9"):
         if k in bh and "bodies_per_s" in bh[k]:
             out[k] = {x: _r(bh[k][x]) for x in ("ms_per_fcompute", "bodies_per_s", "p99")}
+            if k in ("hilbert_theta_0.5", "plain_theta_0.5") and bh[k].get("walk_node_gbs"):
+                # node records read by the walk (20 B per warp node test) per second
+                out[k]["node_gbs"] = _r(bh[k]["walk_node_gbs"], 3)
             if "judge" in bh[k]:
                 j = bh[k]["judge"]
                 out[k]["judge"] = {x: _r(j[x]) if isinstance(j[x], float) else j[x]

@@ -230,13 +230,13 @@ def test_tensor_core_inference_matches_mma_sync(make_engine, count):
     assert d_ref < 3e-2
 
 
-def test_tensor_core_walk_with_zero_network_is_the_group_walk(make_engine):
+@pytest.mark.parametrize("n", [64, 128, 1 << 15])
+def test_tensor_core_walk_with_zero_network_is_the_group_walk(make_engine, n):
     """Zero weights make every correction exactly zero, so the tensor-core
     learned walk equals the plain group walk at the loose ratio on the same
     tree (FP64 nodes) bit for bit -- with the group walk's band-cell records
     in place, and with every group handed to the per-body learned walk
-    (bh.test_cap = 1)."""
-    n = 1 << 15
+    (bh.test_cap = 1); one group (N = 64), two, and many."""
     d = NBodyData.plummer(n, seed=41)
     for cap in (0, 1):
         plain = _bh_engine(make_engine, 1.0 / 0.9)
@@ -251,8 +251,8 @@ def test_tensor_core_walk_with_zero_network_is_the_group_walk(make_engine):
         e.learn_set_weights(np.zeros(M.N_PARAMS, dtype=np.float32))
         f = _forces(e, n)
         rows = e.learn_band_rows()
-        print(f"\ntest_cap {cap}: band rows per body {rows / n:.1f}")
-        assert rows > 0
+        print(f"\nn {n} test_cap {cap}: band rows per body {rows / n:.1f}")
+        assert rows > 0 or n < 1024
         assert np.array_equal(f, f_plain)
 
 
