@@ -288,6 +288,9 @@ uint64_t nbg_launch_count(const nbg_engine* e);
  *       stackless walk) for the mixed-precision Barnes-Hut path,
  *       "bh.group" (64 (default), 32 or 128 bodies per warp in the group
  *       walk; 128 with monopole cells only),
+ *       "bh.walk_npl" (node tests per lane and traversal step of the
+ *       group walk: 2, the default with monopole cells, or 1, the default
+ *       with quadrupole cells),
  *       "bh.build" (0: the reference's kd-median tree, always for FP64;
  *       mixed precision: 1 leaves in Morton order, 2 in Hilbert order (the
  *       default), every node the two halves of its range -- one sort

@@ -313,7 +313,7 @@ __device__ __forceinline__ void group_pair_lo(f2_t xj, f2_t yj, f2_t zj, f2_t mj
 // ratio (the learned correction's band) are recorded in t.cand; a group
 // with more than t.cand_cap of them is handed to the per-body walk.
 template <bool CLAMP, int BPL, int ORDER, int EUNR, bool SMACC, bool FROZEN = false,
-          bool EMIT = false>
+          bool EMIT = false, int NPL = 1>
 __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, double* __restrict__ f,
                                                int n, float eps2v, const TreeState& t,
                                                int stack_cap, unsigned* err,
@@ -516,38 +516,51 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
         __syncwarp();
     };
 
+    // NPL nodes per lane and step: 16 NPL popped entries, 32 NPL children
+    // tested, NPL independent node loads in flight per lane
     while (sp > 0) {
-        const int k = min(sp, 16);
-        int c = 0;
-        if (lane < 2 * k) c = 2 * stack[sp - 1 - (lane >> 1)] + (lane & 1);
+        const int k = min(sp, 16 * NPL);
+        int c[NPL];
+#pragma unroll
+        for (int w = 0; w < NPL; ++w) {
+            const int slot = lane + 32 * w;
+            c[w] = slot < 2 * k ? 2 * stack[sp - 1 - (slot >> 1)] + (slot & 1) : 0;
+        }
         __syncwarp();
         sp -= k;
-        const bool valid = lane < 2 * k && c != 0;
-        bool accept = false, open = false, band = false;
         // issued before a full list is evaluated, which covers their latency;
         // lanes past the popped entries read record 0 (unused, zeroed), and
         // leaves' second moments are zero
-        const float4 nd = __ldg(&t.node4[c]);
-        const float4 nda = FROZEN ? __ldg(&t.node4_acc[c]) : nd;  // acceptance record
-        const float ndm = __ldg(&t.nodem[c]);
-        float4 nq0, nq1;
-        if (ORDER == 2) {
-            nq0 = __ldg(&t.quad[2 * c]);
-            nq1 = __ldg(&t.quad[2 * c + 1]);
+        float4 nd[NPL], nda[NPL], nq0[NPL], nq1[NPL];
+        float ndm[NPL];
+#pragma unroll
+        for (int w = 0; w < NPL; ++w) {
+            nd[w] = __ldg(&t.node4[c[w]]);
+            nda[w] = FROZEN ? __ldg(&t.node4_acc[c[w]]) : nd[w];  // acceptance record
+            ndm[w] = __ldg(&t.nodem[c[w]]);
+            if (ORDER == 2) {
+                nq0[w] = __ldg(&t.quad[2 * c[w]]);
+                nq1[w] = __ldg(&t.quad[2 * c[w] + 1]);
+            }
         }
-        if (lc > kGWList - 32) evaluate();  // room for this step's entries
-        if (ORDER == 2 && qc > kGWQList - 32) evaluate_quad();
-        if (valid) {
-            if (c >= n) {
-                accept = true;
-            } else {
-                const float ex = fmaxf(fabsf(nda.x - cb[0]) - hb[0], 0.f);
-                const float ey = fmaxf(fabsf(nda.y - cb[1]) - hb[1], 0.f);
-                const float ez = fmaxf(fabsf(nda.z - cb[2]) - hb[2], 0.f);
-                const float dmin2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-                accept = dmin2 > nda.w;
-                open = !accept;
-                if constexpr (EMIT) band = accept && dmin2 <= nda.w * t.band2;
+        if (lc > kGWList - 32 * NPL) evaluate();  // room for this step's entries
+        if (ORDER == 2 && qc > kGWQList - 32 * NPL) evaluate_quad();
+        bool accept[NPL], open[NPL], band[NPL];
+#pragma unroll
+        for (int w = 0; w < NPL; ++w) {
+            accept[w] = open[w] = band[w] = false;
+            if (c[w] != 0) {  // slots past the popped entries hold 0
+                if (c[w] >= n) {
+                    accept[w] = true;
+                } else {
+                    const float ex = fmaxf(fabsf(nda[w].x - cb[0]) - hb[0], 0.f);
+                    const float ey = fmaxf(fabsf(nda[w].y - cb[1]) - hb[1], 0.f);
+                    const float ez = fmaxf(fabsf(nda[w].z - cb[2]) - hb[2], 0.f);
+                    const float dmin2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+                    accept[w] = dmin2 > nda[w].w;
+                    open[w] = !accept[w];
+                    if constexpr (EMIT) band[w] = accept[w] && dmin2 <= nda[w].w * t.band2;
+                }
             }
         }
         // every popped entry stands for two tested children, except the root's
@@ -558,60 +571,83 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
             break;
         }
         if constexpr (EMIT) {
-            const unsigned bm = __ballot_sync(0xffffffffu, band);
-            if (ec + __popc(bm) > t.cand_cap) {  // walked body by body instead
+            unsigned bm[NPL];
+            int nb = 0;
+#pragma unroll
+            for (int w = 0; w < NPL; ++w) {
+                bm[w] = __ballot_sync(0xffffffffu, band[w]);
+                nb += __popc(bm[w]);
+            }
+            if (ec + nb > t.cand_cap) {  // walked body by body instead
                 abandoned = true;
                 break;
             }
-            if (band) t.cand[(size_t)gw * t.cand_cap + ec + __popc(bm & lt)] = c;
-            ec += __popc(bm);
+#pragma unroll
+            for (int w = 0; w < NPL; ++w) {
+                if (band[w]) t.cand[(size_t)gw * t.cand_cap + ec + __popc(bm[w] & lt)] = c[w];
+                ec += __popc(bm[w]);
+            }
         }
         // cells with moments go to the quadrupole list (ORDER 2), the rest
         // (leaves, or every node for ORDER 1) to the monopole list
-        const bool to_quad = ORDER == 2 && accept && c < n;
-        const bool to_mono = accept && !to_quad;
-        const unsigned am = __ballot_sync(0xffffffffu, to_mono);
-        const unsigned om = __ballot_sync(0xffffffffu, open);
-        if (to_mono) {
-            const int q = lc + __popc(am & lt);
-            lx[q] = nd.x;
-            ly[q] = nd.y;
-            lz[q] = nd.z;
-            lm[q] = ndm;
-            if constexpr (FROZEN) {  // leaves carry their residuals, cells none
-                const float4 lo = c >= n ? __ldg(&t.leaf_lo[c - n]) : make_float4(0.f, 0.f, 0.f, 0.f);
-                llx[q] = lo.x;
-                lly[q] = lo.y;
-                llz[q] = lo.z;
+#pragma unroll
+        for (int w = 0; w < NPL; ++w) {
+            const bool to_quad = ORDER == 2 && accept[w] && c[w] < n;
+            const bool to_mono = accept[w] && !to_quad;
+            const unsigned am = __ballot_sync(0xffffffffu, to_mono);
+            if (to_mono) {
+                const int q = lc + __popc(am & lt);
+                lx[q] = nd[w].x;
+                ly[q] = nd[w].y;
+                lz[q] = nd[w].z;
+                lm[q] = ndm[w];
+                if constexpr (FROZEN) {  // leaves carry their residuals, cells none
+                    const float4 lo = c[w] >= n ? __ldg(&t.leaf_lo[c[w] - n])
+                                                : make_float4(0.f, 0.f, 0.f, 0.f);
+                    llx[q] = lo.x;
+                    lly[q] = lo.y;
+                    llz[q] = lo.z;
+                }
+            }
+            lc += __popc(am);
+            if (ORDER == 2) {
+                const unsigned aq = __ballot_sync(0xffffffffu, to_quad);
+                if (to_quad) {
+                    float(*v)[kGWQList] = Q.v[warp];
+                    const int q = qc + __popc(aq & lt);
+                    const float4 q0 = nq0[w], q1 = nq1[w];
+                    v[0][q] = nd[w].x;
+                    v[1][q] = nd[w].y;
+                    v[2][q] = nd[w].z;
+                    v[3][q] = ndm[w];
+                    v[4][q] = q0.x;
+                    v[5][q] = q0.y;
+                    v[6][q] = q0.z;
+                    v[7][q] = q0.w;
+                    v[8][q] = q1.x;
+                    v[9][q] = q1.y;
+                    v[10][q] = q1.z;
+                }
+                qc += __popc(aq);
             }
         }
-        lc += __popc(am);
-        if (ORDER == 2) {
-            const unsigned aq = __ballot_sync(0xffffffffu, to_quad);
-            if (to_quad) {
-                float(*v)[kGWQList] = Q.v[warp];
-                const int q = qc + __popc(aq & lt);
-                const float4 q0 = nq0, q1 = nq1;
-                v[0][q] = nd.x;
-                v[1][q] = nd.y;
-                v[2][q] = nd.z;
-                v[3][q] = ndm;
-                v[4][q] = q0.x;
-                v[5][q] = q0.y;
-                v[6][q] = q0.z;
-                v[7][q] = q0.w;
-                v[8][q] = q1.x;
-                v[9][q] = q1.y;
-                v[10][q] = q1.z;
-            }
-            qc += __popc(aq);
+        unsigned om[NPL];
+        int npush = 0;
+#pragma unroll
+        for (int w = 0; w < NPL; ++w) {
+            om[w] = __ballot_sync(0xffffffffu, open[w]);
+            npush += __popc(om[w]);
         }
-        const int npush = __popc(om);
         if (sp + npush > stack_cap) {  // beyond 48 entries per level: reported, never written
             overflow = true;
             break;
         }
-        if (open) stack[sp + __popc(om & lt)] = c;
+        int base = sp;
+#pragma unroll
+        for (int w = 0; w < NPL; ++w) {
+            if (open[w]) stack[base + __popc(om[w] & lt)] = c[w];
+            base += __popc(om[w]);
+        }
         sp += npush;
         peak = max(peak, sp);
         __syncwarp();
@@ -662,7 +698,7 @@ __device__ __forceinline__ void group_walk_one(const double* __restrict__ y, dou
 // leaving a partial wave.  A group's forces do not depend on which warp
 // computes it.
 template <bool CLAMP, int MINB, int BPL, int ORDER, int EUNR = 2, bool SMACC = false,
-          bool FROZEN = false, bool EMIT = false>
+          bool FROZEN = false, bool EMIT = false, int NPL = 1>
 __global__ void __launch_bounds__(kGWThreads, MINB)
 bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n, float eps2v,
                      TreeState t, int stack_cap, unsigned* err) {
@@ -671,8 +707,9 @@ bh_group_walk_kernel(const double* __restrict__ y, double* __restrict__ f, int n
     const int groups = n / (32 * BPL);
     int gw = blockIdx.x * kGWWarps + (threadIdx.x >> 5);
     while (gw < groups) {
-        group_walk_one<CLAMP, BPL, ORDER, EUNR, SMACC, FROZEN, EMIT>(y, f, n, eps2v, t, stack_cap,
-                                                                    err, smem_raw, gw);
+        group_walk_one<CLAMP, BPL, ORDER, EUNR, SMACC, FROZEN, EMIT, NPL>(y, f, n, eps2v, t,
+                                                                         stack_cap, err, smem_raw,
+                                                                         gw);
         int next = 0;
         if (lane == 0) next = (int)atomicAdd(&t.fb_count[1], 1u);
         gw = gridDim.x * kGWWarps + __shfl_sync(0xffffffffu, next, 0);
@@ -1107,9 +1144,11 @@ nbg_status mixed_walk_impl(nbg_engine* e, const double* y, double* f, bool emit)
 #define NBG_GW(C, B) (wb >= 8 ? bh_group_walk_kernel<C, 8, B, 1> : wb >= 6 ? bh_group_walk_kernel<C, 6, B, 1> \
                       : wb >= 5 ? bh_group_walk_kernel<C, 5, B, 1> : bh_group_walk_kernel<C, 4, B, 1>)
         if (emit) {
+            // the default monopole build (two node tests per lane and step),
+            // recording the band cells
             smem += (size_t)kGWThreads * 6 * 2 * sizeof(f2_t);
-            kern = clamp ? bh_group_walk_kernel<true, 5, 2, 1, 2, true, false, true>
-                         : bh_group_walk_kernel<false, 5, 2, 1, 2, true, false, true>;
+            kern = clamp ? bh_group_walk_kernel<true, 5, 2, 1, 2, true, false, true, 2>
+                         : bh_group_walk_kernel<false, 5, 2, 1, 2, true, false, true, 2>;
         } else if (bpl == 4) {
             smem += (size_t)kGWThreads * 6 * 4 * sizeof(f2_t);
             kern = clamp ? bh_group_walk_kernel<true, 4, 4, 1, 2, true>
@@ -1122,6 +1161,11 @@ nbg_status mixed_walk_impl(nbg_engine* e, const double* y, double* f, bool emit)
             kern = clamp ? bh_group_walk_kernel<true, 4, 2, 1, 2, true, true>
                          : bh_group_walk_kernel<false, 4, 2, 1, 2, true, true>;
         }
+        // quadrupole cells: one node test per lane and step by default (two
+        // fill the quadrupole list twice as fast and gain nothing)
+        else if (order == 2 && bpl == 2 && wb <= 3 && e->tune_get("bh.walk_npl", 1) >= 2)
+            kern = clamp ? bh_group_walk_kernel<true, 3, 2, 2, 2, false, false, false, 2>
+                         : bh_group_walk_kernel<false, 3, 2, 2, 2, false, false, false, 2>;
         else if (order == 2 && bpl == 2 && wb <= 3)
             kern = clamp ? bh_group_walk_kernel<true, 3, 2, 2> : bh_group_walk_kernel<false, 3, 2, 2>;
         else if (order == 2)
@@ -1138,6 +1182,11 @@ nbg_status mixed_walk_impl(nbg_engine* e, const double* y, double* f, bool emit)
             else if (wb >= 5 && eu <= 1)
                 kern = clamp ? bh_group_walk_kernel<true, 5, 2, 1, 1, true>
                              : bh_group_walk_kernel<false, 5, 2, 1, 1, true>;
+            else if (wb >= 5 && e->tune_get("bh.walk_npl", 2) >= 2)
+                // two node tests per lane and step (the default): half the
+                // dependent traversal steps, two loads in flight
+                kern = clamp ? bh_group_walk_kernel<true, 5, 2, 1, 2, true, false, false, 2>
+                             : bh_group_walk_kernel<false, 5, 2, 1, 2, true, false, false, 2>;
             else
                 kern = clamp ? (wb >= 5 ? bh_group_walk_kernel<true, 5, 2, 1, 2, true>
                                         : bh_group_walk_kernel<true, 4, 2, 1, 2, true>)
