@@ -49,6 +49,7 @@ constexpr int kTcCols = 64;
 constexpr int kTcBlocksPerSm = 6;    // as shared memory allows; 6 x 64 of the SM's 512 columns
 constexpr int kGroupBodies = 64;     // bodies of a group (the default group walk)
 constexpr int kCellChunk = 64;       // band cells staged in shared memory at a time
+static_assert(kCellChunk == 64, "the full-chunk index split is a shift by 6");
 // dynamic shared memory per CTA at least this: at most 8 CTAs per SM, so
 // every resident CTA's TMEM allocation (8 x 64 = 512 columns) succeeds
 constexpr size_t kTcSmemFloor = 26 * 1024;
@@ -308,7 +309,8 @@ learned_tc_kernel(double* __restrict__ f, int n, int groups, TreeState t,
                     bool flag = false;
                     int ci = 0, bi = 0;
                     if (p < items) {
-                        bi = p / nc;
+                        // full chunks (all but a group's last) by shift and mask
+                        bi = nc == kCellChunk ? p >> 6 : p / nc;
                         ci = p - bi * nc;
                         const float4 nd = S.cnode[ci];
                         const float4 me = S.body[bi];
