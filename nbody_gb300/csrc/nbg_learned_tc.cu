@@ -136,17 +136,26 @@ __device__ __forceinline__ uint32_t gelu2_bf16(f2_t acc, f2_t bias) {
 __device__ __forceinline__ void hidden_to_operand(uint32_t taddr, const float* bias, uint32_t* a2,
                                                   int row, float* dump) {
     unsigned char* base = reinterpret_cast<unsigned char*>(a2);
+    const float4* bias4 = reinterpret_cast<const float4*>(bias);  // 16-byte aligned
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         float v[16];
         tc::ld16(taddr + 16 * j, v);
         if (dump != nullptr)
             for (int q = 0; q < 16; ++q) dump[16 * j + q] = v[q];
+        float b[16];  // the 16 columns' biases, four 128-bit shared loads
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float4 w = bias4[4 * j + q];
+            b[4 * q] = w.x;
+            b[4 * q + 1] = w.y;
+            b[4 * q + 2] = w.z;
+            b[4 * q + 3] = w.w;
+        }
         uint32_t p[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i)
-            p[i] = gelu2_bf16(f2_pack(v[2 * i], v[2 * i + 1]),
-                              f2_pack(bias[16 * j + 2 * i], bias[16 * j + 2 * i + 1]));
+            p[i] = gelu2_bf16(f2_pack(v[2 * i], v[2 * i + 1]), f2_pack(b[2 * i], b[2 * i + 1]));
         *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, 16 * j, 64)) =
             make_uint4(p[0], p[1], p[2], p[3]);
         *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, 16 * j + 8, 64)) =
