@@ -467,27 +467,47 @@ __global__ void ens_sym_reduce_kernel(const int* __restrict__ sys, const long lo
 
 // Candidate update y_new = y + dt sum b2_i k_i and per-system error
 // max |dt sum (b2_i - b1_i) k_i| (as ordered bits, atomicMax).
+// A warp covers 32 consecutive bodies, which belong to one system or a few
+// neighbouring ones (bodies are stored system by system): a segmented max
+// over the warp leaves each system's maximum in its first lane, and only
+// those lanes reach the system's error word (max is order-free, so the
+// result does not depend on the schedule).
 __global__ void ens_error_kernel(const double* __restrict__ y, const int* __restrict__ sys,
                                  const double* __restrict__ dt, KPtrs kp, size_t B,
                                  double* __restrict__ ynew, unsigned long long* __restrict__ err) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < B;
-         i += (size_t)gridDim.x * blockDim.x) {
-        const int s = sys[i];
-        const double h = dt[s];
+    const int lane = threadIdx.x & 31;
+    const size_t warp0 = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) & ~(size_t)31;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t base = warp0; base < B; base += stride) {  // warp-uniform
+        const size_t i = base + lane;
+        const bool live = i < B;
+        const int s = live ? sys[i] : -1;
         double emax = 0.0;
+        if (live) {
+            const double h = dt[s];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            double acc_b2 = 0.0, acc_e = 0.0;
+            for (int c = 0; c < 6; ++c) {
+                double acc_b2 = 0.0, acc_e = 0.0;
 #pragma unroll
-            for (int j = 0; j < kStagesRK; ++j) {
-                const double kv = kp.k[j][c * B + i];
-                acc_b2 = fma(c_b2[j], kv, acc_b2);
-                acc_e = fma(c_b2[j] - c_b1[j], kv, acc_e);
+                for (int j = 0; j < kStagesRK; ++j) {
+                    const double kv = kp.k[j][c * B + i];
+                    acc_b2 = fma(c_b2[j], kv, acc_b2);
+                    acc_e = fma(c_b2[j] - c_b1[j], kv, acc_e);
+                }
+                ynew[c * B + i] = fma(h, acc_b2, y[c * B + i]);
+                emax = fmax(emax, fabs(h * acc_e));
             }
-            ynew[c * B + i] = fma(h, acc_b2, y[c * B + i]);
-            emax = fmax(emax, fabs(h * acc_e));
         }
-        atomicMax(&err[s], (unsigned long long)__double_as_longlong(emax));
+        // segmented suffix max: lanes of one system are contiguous
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double w = __shfl_down_sync(0xffffffffu, emax, o);
+            const int sw = __shfl_down_sync(0xffffffffu, s, o);
+            if (lane + o < 32 && sw == s) emax = fmax(emax, w);
+        }
+        const int sp = __shfl_up_sync(0xffffffffu, s, 1);
+        if (live && (lane == 0 || sp != s))
+            atomicMax(&err[s], (unsigned long long)__double_as_longlong(emax));
     }
 }
 
