@@ -215,6 +215,16 @@ inline nbody_engine* nbody_create_engine_gb300(const QVariantMap& param)
 	{
 		nbg_tune_set(e->handle(), "learned.judge", param.value("learned_judge").toBool() ? 1 : 0);
 	}
+	if(param.contains("learned_judge_samples"))
+	{
+		const int samples = param.value("learned_judge_samples").toInt();
+		if(samples < 1)	// the Python factory's answer to the same value
+		{
+			delete e;
+			return nullptr;
+		}
+		nbg_tune_set(e->handle(), "learned.judge_samples", samples);
+	}
 	return e;
 }
 
