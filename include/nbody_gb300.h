@@ -402,7 +402,9 @@ nbg_status nbg_ensemble_statistics(nbg_ensemble* s, double* out);
 /* Tuning keys "ensemble.symmetric" (1, the default: every unordered pair of
  * a system evaluated once for both bodies, the reaction sums kept as
  * per-range partials and added in a fixed order, so results stay
- * bit-reproducible; 0: the one-sided kernel), "ensemble.pairs_per_lane" (1
+ * bit-reproducible; the partials take sum_s ceil(N_s / (256 G)) N_s floats
+ * per component, and above 8 GiB the one-sided kernel runs instead; 0: the
+ * one-sided kernel), "ensemble.pairs_per_lane" (1
  * or 2: i-tile of 256 or 512 bodies per work unit), "ensemble.blocks_per_sm"
  * (0 = as many as fit),
  * "ensemble.unroll" (2, 4 or 8: j-loop unroll of the force kernel),

@@ -707,10 +707,25 @@ nbg_status ens_configure_sym(nbg_ensemble* s) {
 // 256 G bodies, CTAs per SM; "ensemble.symmetric" 1, the default: every
 // unordered pair once); drops a captured step graph built for an older
 // shape.
+// The symmetric kernel's partials take sum_s ceil(N_s / RA) N_s floats per
+// component: small for many small systems (300 MB for 2048 systems of up to
+// 4096 bodies), but growing as N^2 / RA for one large system; above this
+// size the ensemble uses the one-sided kernel, which needs no such buffer.
+constexpr size_t kEnsSymMaxPartialBytes = size_t(8) << 30;
+
 nbg_status ens_configure(nbg_ensemble* s) {
     nbg_engine* e = s->eng;
     s->G = (int)std::max<int64_t>(1, std::min<int64_t>(2, e->tune_get("ensemble.pairs_per_lane", 2)));
     s->sym = e->tune_get("ensemble.symmetric", 1) != 0;
+    if (s->sym) {
+        const long long ra = kEnsThreads * 2 * s->G;
+        size_t floats = 0;
+        for (int sI = 0; sI < s->nsys; ++sI) {
+            const long long n = s->h_cnt[sI];
+            floats += (size_t)((n + ra - 1) / ra) * (size_t)n;
+        }
+        if (3 * floats * sizeof(float) > kEnsSymMaxPartialBytes) s->sym = false;
+    }
     if (s->sym) {
         NBG_CUDA(e, cudaStreamSynchronize(e->stream));
         nbg_status st = ens_configure_sym(s);
