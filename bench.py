@@ -914,8 +914,8 @@ def run_gb300(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "n": n, "softening": SOFTENING, "dt": DT,
-                       "integrator": "rk4", "precision": "f32 pairs, two-sum tiles, f64 state",
-                       "l2": "flushed between timed steps (256 MB write)",
+                       "integrator": "rk4",
+                       "l2": "flushed between steps (256 MB write)",
                        "parallelism": f"replicas x{world}",
                        "tuning": tuning["best"]},
             "roofline": {"bound": "fp32", "achieved": _r(achieved_tflops),
