@@ -199,8 +199,11 @@ nbg_status nbg_bh_fallback_groups(nbg_engine* e, uint64_t* groups);
  * "learned.walk" 1 (default): the default group walk (64-body groups)
  * records each group's band cells and the network evaluates the band
  * (body, cell) rows in 128-row tiles on the tcgen05 tensor cores, the
- * per-body sums taken in a fixed order; 0: the warp-coherent per-body walk
- * with one mma.sync batch per band cell; "learned.group" one sample per
+ * per-body sums taken in a fixed order (with other walk settings --
+ * "bh.walk" 0, "bh.group" 32 or 128, "bh.order" 2, "bh.acc_smem" 0,
+ * "bh.freeze_within_step" 1 -- the learned path takes the per-body walk);
+ * 0: the warp-coherent per-body walk with one mma.sync batch per band
+ * cell; "learned.group" one sample per
  * (body, cell) (0, default) or per (warp, cell) at the warp centroid (1, on
  * the per-body walk); "learned.weighted" (0 default, 1: training loss
  * weighted by the cell's force scale (m / s^2)^2).

@@ -811,10 +811,14 @@ nbg_status learned_walk(nbg_engine* e, const double* y, double* f) {
     TreeState* t = e->tree;
     const int n = (int)e->count;
     // "learned.walk": 1 (default) the group walk with the network on the
-    // tcgen05 tensor cores (nbg_learned_tc.cu); 0 the warp-coherent per-body
-    // walk below, one mma.sync batch per band cell
+    // tcgen05 tensor cores (nbg_learned_tc.cu), which runs on the default
+    // group walk only (64-body groups, monopole cells, acceptance not frozen);
+    // 0, or any other walk setting: the warp-coherent per-body walk below,
+    // one mma.sync batch per band cell
     if (e->tune_get("learned.walk", 1) == 1 && e->tune_get("learned.group", 0) == 0 &&
-        e->tune_get("bh.walk", 1) == 1 && n >= 64)
+        e->tune_get("bh.walk", 1) == 1 && e->tune_get("bh.group", 64) == 64 &&
+        e->tune_get("bh.order", 1) == 1 && e->tune_get("bh.freeze_within_step", 0) == 0 &&
+        e->tune_get("bh.acc_smem", 1) != 0 && n >= 64)
         return learned_tc_walk(e, y, f);
     const double lam_l = e->params.distance_to_node_radius_ratio;
     const double lam_t = e->params.learned_tight_ratio;

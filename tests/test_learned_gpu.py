@@ -256,6 +256,30 @@ def test_tensor_core_walk_with_zero_network_is_the_group_walk(make_engine, n):
         assert np.array_equal(f, f_plain)
 
 
+@pytest.mark.parametrize("tune", [{"bh.group": 32}, {"bh.order": 2},
+                                  {"bh.freeze_within_step": 1}],
+                         ids=["group32", "quadrupole", "frozen"])
+def test_other_walk_settings_take_the_per_body_learned_walk(make_engine, tune):
+    """The tensor-core path needs the default group walk; with other walk
+    settings the learned engine takes the per-body (warp-coherent) learned
+    walk, the same forces as learned.walk = 0 bit for bit."""
+    n = 1 << 13
+    d = NBodyData.plummer(n, seed=43)
+    w = _random_weights(6, scale=0.05)
+    out = []
+    for walk in (1, 0):
+        e = _bh_engine(make_engine, 1.0 / 0.9, learned=True)
+        e.tune_set("learned.judge", 0)
+        e.tune_set("learned.walk", walk)
+        for k, v in tune.items():
+            e.tune_set(k, v)
+        assert e.init(d)
+        e.learn_set_weights(w)
+        out.append(_forces(e, n))
+    assert np.all(np.isfinite(out[0]))
+    assert np.array_equal(out[0], out[1])
+
+
 def test_tensor_core_walk_vs_plain(make_engine, oracle, trained):
     """The trained network on the tensor-core group walk at theta = 0.9,
     judged by the FP64 direct sum on a snapshot the network never saw: a
