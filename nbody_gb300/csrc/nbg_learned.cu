@@ -159,10 +159,14 @@ struct WarpStage {               // per-warp staging, BF16 pairs packed in u32
     uint32_t d1T[64 * 16];       // dZ1^T [64][32]
 };
 
+// Each warp sums its samples' gradients into its own slice (wacc[warp]), so
+// no two warps add to one word; the block adds the slices in warp order at
+// the end.
 struct TrainSmem {
     uint2 frag[kFragWords];
     float bias[kBias];
-    float gacc[kParams + 5];
+    float wacc[kTrainWarps][kParams + 5];
+    double lsum[kTrainWarps];
     WarpStage ws[kTrainWarps];
 };
 
@@ -207,18 +211,19 @@ __device__ __forceinline__ uint2 frag_B_T(const uint32_t* T, int n0, int k0, int
     return b;
 }
 
-// gacc[off + r * ld + c] += C-tile (16 x 8 at r0, c0)
+// gacc[off + r * ld + c] += C-tile (16 x 8 at r0, c0); gacc is the warp's
+// own slice and the lanes' words are distinct, so plain adds
 __device__ __forceinline__ void acc_tile(float* gacc, int off, int ld, int r0, int c0, int cmax,
                                          const float c[4], int lane) {
     const int g = lane >> 2, t = lane & 3;
     const int cc = c0 + 2 * t;
     if (cc < cmax) {
-        atomicAdd(&gacc[off + (r0 + g) * ld + cc], c[0]);
-        atomicAdd(&gacc[off + (r0 + g + 8) * ld + cc], c[2]);
+        gacc[off + (r0 + g) * ld + cc] += c[0];
+        gacc[off + (r0 + g + 8) * ld + cc] += c[2];
     }
     if (cc + 1 < cmax) {
-        atomicAdd(&gacc[off + (r0 + g) * ld + cc + 1], c[1]);
-        atomicAdd(&gacc[off + (r0 + g + 8) * ld + cc + 1], c[3]);
+        gacc[off + (r0 + g) * ld + cc + 1] += c[1];
+        gacc[off + (r0 + g + 8) * ld + cc + 1] += c[3];
     }
 }
 
@@ -237,8 +242,8 @@ __device__ __forceinline__ void acc_colsum(float* gacc, int off, int cmax, const
         }
         if (lane < 4) {
             const int col = 8 * nt + 2 * t;
-            if (col < cmax) atomicAdd(&gacc[off + col], s0);
-            if (col + 1 < cmax) atomicAdd(&gacc[off + col + 1], s1);
+            if (col < cmax) gacc[off + col] += s0;
+            if (col + 1 < cmax) gacc[off + col + 1] += s1;
         }
     }
 }
@@ -246,17 +251,19 @@ __device__ __forceinline__ void acc_colsum(float* gacc, int off, int cmax, const
 __global__ void __launch_bounds__(kTrainWarps * 32)
 train_kernel(const float* __restrict__ x, const float* __restrict__ tg, const int* __restrict__ order,
              size_t b0, size_t bsize, const uint2* __restrict__ frag_g,
-             const float* __restrict__ bias_g, float* __restrict__ grad, double* __restrict__ loss,
-             float wnorm) {
+             const float* __restrict__ bias_g, float* __restrict__ grad_part,
+             double* __restrict__ loss_part, float wnorm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
     for (int i = threadIdx.x; i < kFragWords; i += blockDim.x) S.frag[i] = frag_g[i];
     for (int i = threadIdx.x; i < kBias; i += blockDim.x) S.bias[i] = bias_g[i];
-    for (int i = threadIdx.x; i < kParams + 5; i += blockDim.x) S.gacc[i] = 0.f;
+    for (int i = threadIdx.x; i < kTrainWarps * (kParams + 5); i += blockDim.x)
+        (&S.wacc[0][0])[i] = 0.f;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = lane >> 2, t = lane & 3;
     WarpStage& W = S.ws[warp];
+    float* gacc = S.wacc[warp];  // this warp's gradient sums
     const float inv_b = 1.f / (float)bsize;
     double sq = 0.0;
     const size_t chunks = (bsize + 31) / 32;
@@ -368,8 +375,8 @@ train_kernel(const float* __restrict__ x, const float* __restrict__ tg, const in
             for (int nt = 0; nt < 8; ++nt)
                 for (int q = 0; q < 4; ++q) dz[m][nt][q] *= gelu_grad(z2[m][nt][q]);
         stage_T<8>(W.d2T, dz, lane);
-        acc_colsum<8>(S.gacc, kOffB2, kH, dz, lane);
-        acc_colsum<1>(S.gacc, kOffB3, kOut, d3, lane);
+        acc_colsum<8>(gacc, kOffB2, kH, dz, lane);
+        acc_colsum<1>(gacc, kOffB3, kOut, d3, lane);
         // ---- dA1 = dZ2 W2^T ; dZ1 = dA1 * gelu'(Z1) ----
         uint32_t adz[2][4][4];
         for (int m = 0; m < 2; ++m)
@@ -392,7 +399,7 @@ train_kernel(const float* __restrict__ x, const float* __restrict__ tg, const in
             for (int nt = 0; nt < 8; ++nt)
                 for (int q = 0; q < 4; ++q) d1[m][nt][q] *= gelu_grad(z1[m][nt][q]);
         stage_T<8>(W.d1T, d1, lane);
-        acc_colsum<8>(S.gacc, kOffB1, kH, d1, lane);
+        acc_colsum<8>(gacc, kOffB1, kH, d1, lane);
         __syncwarp();
         // ---- weight gradients: K = the 32 samples ----
         // dW3[h][c] = A2^T dY : M = 64 (4 tiles), N = 8, K = 32
@@ -403,7 +410,7 @@ train_kernel(const float* __restrict__ x, const float* __restrict__ tg, const in
                 frag_A_T(W.a2T, 16 * mt, 16 * kt, lane, a);
                 mma_bf16(c, a, frag_B_T(W.d3T, 0, 16 * kt, lane));
             }
-            acc_tile(S.gacc, kOffW3, kOut, 16 * mt, 0, kOut, c, lane);
+            acc_tile(gacc, kOffW3, kOut, 16 * mt, 0, kOut, c, lane);
         }
         // dW2[h][h'] = A1^T dZ2 : M = 64, N = 64, K = 32
         for (int mt = 0; mt < 4; ++mt)
@@ -414,7 +421,7 @@ train_kernel(const float* __restrict__ x, const float* __restrict__ tg, const in
                     frag_A_T(W.a1T, 16 * mt, 16 * kt, lane, a);
                     mma_bf16(c, a, frag_B_T(W.d2T, 8 * nt, 16 * kt, lane));
                 }
-                acc_tile(S.gacc, kOffW2, kH, 16 * mt, 8 * nt, kH, c, lane);
+                acc_tile(gacc, kOffW2, kH, 16 * mt, 8 * nt, kH, c, lane);
             }
         // dW1[f][h] = X^T dZ1 : M = 16, N = 64, K = 32
         for (int nt = 0; nt < 8; ++nt) {
@@ -424,16 +431,42 @@ train_kernel(const float* __restrict__ x, const float* __restrict__ tg, const in
                 frag_A_T(W.xT, 0, 16 * kt, lane, a);
                 mma_bf16(c, a, frag_B_T(W.d1T, 8 * nt, 16 * kt, lane));
             }
-            acc_tile(S.gacc, kOffW1, kH, 0, 8 * nt, kH, c, lane);
+            acc_tile(gacc, kOffW1, kH, 0, 8 * nt, kH, c, lane);
         }
         __syncwarp();
     }
-    // loss: warp sum -> one atomic per warp
+    // the block's loss and gradient: the warps' sums in warp order
     for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
-    if (lane == 0) atomicAdd(&loss[0], sq);
+    if (lane == 0) S.lsum[warp] = sq;
     __syncthreads();
-    for (int i = threadIdx.x; i < kParams; i += blockDim.x)
-        if (S.gacc[i] != 0.f) atomicAdd(&grad[i], S.gacc[i]);
+    for (int i = threadIdx.x; i < kParams; i += blockDim.x) {
+        float v = S.wacc[0][i];
+#pragma unroll
+        for (int w = 1; w < kTrainWarps; ++w) v += S.wacc[w][i];
+        grad_part[(size_t)blockIdx.x * kParams + i] = v;
+    }
+    if (threadIdx.x == 0) {
+        double l = S.lsum[0];
+        for (int w = 1; w < kTrainWarps; ++w) l += S.lsum[w];
+        loss_part[blockIdx.x] = l;
+    }
+}
+
+// grad = the pass's gradient (the blocks' partials in block order); the
+// pass's loss is added to loss[0].
+__global__ void grad_reduce_kernel(const float* __restrict__ grad_part, int blocks,
+                                   float* __restrict__ grad, const double* __restrict__ loss_part,
+                                   double* __restrict__ loss) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kParams; i += gridDim.x * blockDim.x) {
+        float v = grad_part[i];
+        for (int b = 1; b < blocks; ++b) v += grad_part[(size_t)b * kParams + i];
+        grad[i] = v;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        double l = 0.0;
+        for (int b = 0; b < blocks; ++b) l += loss_part[b];
+        loss[0] += l;
+    }
 }
 
 __global__ void adam_kernel(float* w, float* grad, float* m1, float* m2, float lr, float b1,
@@ -454,12 +487,18 @@ __global__ void adam_kernel(float* w, float* grad, float* m1, float* m2, float l
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int next_down_i(int idx) { return (idx >> (__ffs(~idx) - 1)) + 1; }
 
-// One thread per sampled leaf (index in [n, 2n)): walk at the loose ratio and
-// record every accepted internal node inside the band whose subtree holds at
-// most 2^max_level_leaves_log2 bodies.
+// One thread per sampled leaf k (index in [n, 2n)): walk at the loose ratio
+// and find every accepted internal node inside the band whose subtree holds
+// at most 2^max_level_leaves_log2 bodies.  The first pass (WRITE false)
+// counts them into counts[k]; the second writes leaf k's pairs, in walk
+// order, from slot first[k] (the counts' exclusive prefix sum), those below
+// cap.  So the sample store's order and content follow the sampled leaves'
+// order, whatever the schedule.
+template <bool WRITE>
 __global__ void sample_pairs_kernel(const int* __restrict__ leaves, int nb, TreeState t, int n,
                                     float band2, int max_level_leaves_log2, int levels,
-                                    int* __restrict__ pairs, unsigned long long* __restrict__ cnt,
+                                    int* __restrict__ pairs, unsigned* __restrict__ counts,
+                                    const unsigned long long* __restrict__ first,
                                     unsigned long long cap) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nb) return;
@@ -468,6 +507,8 @@ __global__ void sample_pairs_kernel(const int* __restrict__ leaves, int nb, Tree
     int curr = 1;
     const int sz = (int)t.size;
     int steps = 0;
+    unsigned found = 0;
+    const unsigned long long slot0 = WRITE ? first[k] : 0ull;
     do {
         const float4 nd = t.node4[curr];
         const float dx = nd.x - me.x, dy = nd.y - me.y, dz = nd.z - me.z;
@@ -476,11 +517,14 @@ __global__ void sample_pairs_kernel(const int* __restrict__ leaves, int nb, Tree
             if (curr < n && d2 <= nd.w * band2) {
                 const int lv = 31 - __clz(curr);
                 if (levels - lv <= max_level_leaves_log2) {
-                    const unsigned long long slot = atomicAdd(cnt, 1ull);
-                    if (slot < cap) {
-                        pairs[2 * slot] = leaf;
-                        pairs[2 * slot + 1] = curr;
+                    if (WRITE) {
+                        const unsigned long long slot = slot0 + found;
+                        if (slot < cap) {
+                            pairs[2 * slot] = leaf;
+                            pairs[2 * slot + 1] = curr;
+                        }
                     }
+                    ++found;
                 }
             }
             curr = next_down_i(curr);
@@ -488,6 +532,7 @@ __global__ void sample_pairs_kernel(const int* __restrict__ leaves, int nb, Tree
             curr = (2 * curr < sz) ? 2 * curr : next_down_i(curr);
         }
     } while (curr != 1 && ++steps <= sz);
+    if (!WRITE) counts[k] = found;
 }
 
 // One warp per pair: exact subtree acceleration (FP64) minus the monopole,
@@ -794,8 +839,8 @@ bool learned_ready(const nbg_engine* e) { return e->learn != nullptr && e->learn
 void learn_destroy(nbg_engine* e) {
     LearnState* L = e->learn;
     if (L == nullptr) return;
-    void* ptrs[] = {L->w, L->grad, L->m1, L->m2, L->frag, L->bias, L->loss,
-                    L->x, L->t, L->meta, L->pairs, L->pair_count, L->mom};
+    void* ptrs[] = {L->w, L->grad, L->m1, L->m2, L->frag, L->bias, L->loss, L->grad_part,
+                    L->loss_part, L->x, L->t, L->meta, L->pairs, L->mom};
     for (void* p : ptrs) cudaFree(p);
     learned_tc_free(L);
     delete L;
@@ -962,8 +1007,6 @@ nbg_status nbg_learn_generate(nbg_engine* e, size_t max_samples, uint64_t seed,
     cudaFree(L->pairs);
     L->pairs = nullptr;
     NBG_CUDA(e, cudaMalloc(&L->pairs, max_samples * 2 * sizeof(int)));
-    if (L->pair_count == nullptr) NBG_CUDA(e, cudaMalloc(&L->pair_count, sizeof(unsigned long long)));
-    NBG_CUDA(e, cudaMemsetAsync(L->pair_count, 0, sizeof(unsigned long long), e->stream));
     // sampled bodies: a seeded random permutation of leaves, enough to fill
     std::vector<int> leaves(n);
     for (int i = 0; i < n; ++i) leaves[i] = n + i;
@@ -982,13 +1025,31 @@ nbg_status nbg_learn_generate(nbg_engine* e, size_t max_samples, uint64_t seed,
     const double lam_l = e->params.distance_to_node_radius_ratio;
     const double lam_t = e->params.learned_tight_ratio;
     const float band2 = (float)((lam_t / lam_l) * (lam_t / lam_l));
-    sample_pairs_kernel<<<(nb + 127) / 128, 128, 0, e->stream>>>(
-        d_bodies, nb, *t, n, band2, max_subtree_log2, t->levels, L->pairs, L->pair_count,
-        (unsigned long long)max_samples);
+    // pairs per sampled leaf, their exclusive prefix sum (on the host), then
+    // the pairs at those slots
+    DevScratch s_counts, s_first;
+    NBG_CUDA(e, cudaMalloc(&s_counts.p, nb * sizeof(unsigned)));
+    NBG_CUDA(e, cudaMalloc(&s_first.p, nb * sizeof(unsigned long long)));
+    sample_pairs_kernel<false><<<(nb + 127) / 128, 128, 0, e->stream>>>(
+        d_bodies, nb, *t, n, band2, max_subtree_log2, t->levels, nullptr, s_counts.as<unsigned>(),
+        nullptr, 0ull);
     NBG_LAUNCHED(e, "sample_pairs_kernel");
-    unsigned long long got = 0;
-    NBG_CUDA(e, cudaMemcpyAsync(&got, L->pair_count, sizeof(got), cudaMemcpyDeviceToHost, e->stream));
+    std::vector<unsigned> counts(nb);
+    NBG_CUDA(e, cudaMemcpyAsync(counts.data(), s_counts.p, nb * sizeof(unsigned),
+                                cudaMemcpyDeviceToHost, e->stream));
     NBG_CUDA(e, cudaStreamSynchronize(e->stream));
+    std::vector<unsigned long long> first(nb);
+    unsigned long long got = 0;
+    for (int k = 0; k < nb; ++k) {
+        first[k] = got;
+        got += counts[k];
+    }
+    NBG_CUDA(e, cudaMemcpyAsync(s_first.p, first.data(), nb * sizeof(unsigned long long),
+                                cudaMemcpyHostToDevice, e->stream));
+    sample_pairs_kernel<true><<<(nb + 127) / 128, 128, 0, e->stream>>>(
+        d_bodies, nb, *t, n, band2, max_subtree_log2, t->levels, L->pairs, nullptr,
+        s_first.as<unsigned long long>(), (unsigned long long)max_samples);
+    NBG_LAUNCHED(e, "sample_pairs_kernel");
     const size_t np = std::min((size_t)got, max_samples);
     if (np > 0) {
         const double eps2 = e->params.softening * e->params.softening;
@@ -1025,8 +1086,9 @@ nbg_status nbg_learn_clear_samples(nbg_engine* e) {
     return NBG_OK;
 }
 
-// One pass of forward + backward over `order[b0 .. b0 + bsize)` of (x, t);
-// grad and loss accumulate on the device.
+// One pass of forward + backward over `order[b0 .. b0 + bsize)` of (x, t):
+// grad = the pass's gradient, loss[0] += its squared error, both summed in
+// a fixed order (equal inputs give equal results).
 static nbg_status run_train_pass(nbg_engine* e, const float* x, const float* t, const int* order,
                                  size_t b0, size_t bsize, float wnorm = 0.f) {
     LearnState* L = e->learn;
@@ -1037,9 +1099,23 @@ static nbg_status run_train_pass(nbg_engine* e, const float* x, const float* t, 
     unsigned grid = (unsigned)std::min<size_t>((chunks + kTrainWarps - 1) / kTrainWarps,
                                                (size_t)e->sm_count);
     if (grid < 1) grid = 1;
-    train_kernel<<<grid, kTrainWarps * 32, smem, e->stream>>>(x, t, order, b0, bsize, L->frag,
-                                                             L->bias, L->grad, L->loss, wnorm);
+    if ((int)grid > L->part_blocks) {
+        cudaFree(L->grad_part);
+        cudaFree(L->loss_part);
+        L->grad_part = nullptr;
+        L->loss_part = nullptr;
+        L->part_blocks = 0;
+        NBG_CUDA(e, cudaMalloc(&L->grad_part, (size_t)grid * kParams * sizeof(float)));
+        NBG_CUDA(e, cudaMalloc(&L->loss_part, (size_t)grid * sizeof(double)));
+        L->part_blocks = (int)grid;
+    }
+    train_kernel<<<grid, kTrainWarps * 32, smem, e->stream>>>(
+        x, t, order, b0, bsize, L->frag, L->bias, L->grad_part, L->loss_part, wnorm);
     NBG_LAUNCHED(e, "train_kernel");
+    grad_reduce_kernel<<<(kParams + 255) / 256, 256, 0, e->stream>>>(L->grad_part, (int)grid,
+                                                                       L->grad, L->loss_part,
+                                                                       L->loss);
+    NBG_LAUNCHED(e, "grad_reduce_kernel");
     return NBG_OK;
 }
 

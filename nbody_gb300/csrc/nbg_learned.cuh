@@ -32,6 +32,11 @@ struct LearnState {
     uint2* frag = nullptr;   // fragment-ordered BF16 weights [kFragWords]
     float* bias = nullptr;   // padded biases [kBias]
     double* loss = nullptr;  // [2] sum of squared error, sample count
+    // per-block gradient and loss partials of one training pass, added in
+    // block order (no atomics: a pass's gradient does not depend on the schedule)
+    float* grad_part = nullptr;   // [part_blocks][kParams]
+    double* loss_part = nullptr;  // [part_blocks]
+    int part_blocks = 0;
     int64_t adam_step = 0;
     bool has_weights = false;
     // training samples
@@ -41,7 +46,6 @@ struct LearnState {
     size_t count = 0, cap = 0;
     // sample-generation scratch
     int* pairs = nullptr;    // [cap][2]
-    unsigned long long* pair_count = nullptr;
     double* mom = nullptr;   // [6][size] FP64 second moments of the current tree
     size_t mom_size = 0;
     // per-step judge (nbg_judge.cu): the step judged last, the step sent to

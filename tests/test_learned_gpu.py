@@ -137,6 +137,29 @@ def trained(request):
     return res
 
 
+def test_samples_and_training_repeat_bit_for_bit(make_engine):
+    """Sample generation (pairs compacted in sampled-leaf order) and training
+    (per-warp gradient sums added in warp and block order, no atomics) give
+    the same samples and the same weights on every run with the same seeds."""
+    runs = []
+    for _ in range(2):
+        e = _bh_engine(make_engine, 1.0 / 0.9)
+        total = 0
+        for i, kind in enumerate(("plummer", "cube")):
+            d = NBodyData.plummer(1 << 14, seed=60 + i) if kind == "plummer" else \
+                NBodyData.uniform_cube(1 << 14, side=2.0, seed=60 + i)
+            assert e.init(d)
+            total += e.learn_generate(200_000, seed=70 + i)
+        x, t, meta = e.learn_read_samples(0, total)
+        tr, va = e.learn_train(2, batch=4096, lr=3e-3, seed=9)
+        runs.append((total, x, t, meta, tr, va, e.learn_get_weights()))
+    (n0, x0, t0, m0, tr0, va0, w0), (n1, x1, t1, m1, tr1, va1, w1) = runs
+    assert n0 == n1 and n0 > 10_000
+    assert np.array_equal(m0, m1) and np.array_equal(x0, x1) and np.array_equal(t0, t1)
+    assert tr0 == tr1 and va0 == va1
+    assert np.array_equal(w0, w1)
+
+
 def test_training_fits_the_residual(trained):
     w, var0, tr, va = trained
     assert np.all(np.isfinite(w))
