@@ -224,7 +224,8 @@ nbg_status nbg_learn_init_weights(nbg_engine* e, uint64_t seed);
 /* Build the tree of the engine's current state and append up to max_samples
  * (features, target) samples: exact subtree sums for in-band interactions of
  * randomly chosen bodies; cells with more than 2^max_subtree_log2 bodies
- * are skipped. */
+ * are skipped.  The samples follow the seeded order of the chosen bodies, so
+ * equal states and seeds give equal samples. */
 nbg_status nbg_learn_generate(nbg_engine* e, size_t max_samples, uint64_t seed,
                               int max_subtree_log2, size_t* produced);
 size_t nbg_learn_sample_count(const nbg_engine* e);
@@ -234,7 +235,8 @@ nbg_status nbg_learn_read_samples(nbg_engine* e, size_t offset, size_t count, fl
                                   float* t, int* meta);
 nbg_status nbg_learn_clear_samples(nbg_engine* e);
 /* Adam on the stored samples (MSE), cosine-decayed learning rate; a seeded
- * val_fraction of the samples is held out and scored at the end. */
+ * val_fraction of the samples is held out and scored at the end.  Gradients
+ * are summed in a fixed order: equal samples and seeds give equal weights. */
 nbg_status nbg_learn_train(nbg_engine* e, int epochs, size_t batch, double lr, uint64_t seed,
                            double val_fraction, double* train_mse, double* val_mse);
 /* Sum of squared errors and the gradient of the mean loss over host samples

@@ -18,12 +18,15 @@
 // Q u/|u| and the mass-centre offset (apply_head), so its correction turns
 // with the cell.  The engine generates training samples from its own trees
 // (exact subtree sums over contiguous leaf ranges), trains the network with BF16
-// tensor-core forward/backward kernels and Adam, and applies it inside the
-// FP32 walk.  Two inference modes (per-body is the default):
-//   per-body  (learned.group = 0): one MLP sample per (body, cell) pair;
-//   group     (learned.group = 1): one sample per (warp, cell) at the warp's
-//             centroid, 32 cells batched per tensor-core call, the correction
-//             shared by the warp's 32 neighbouring bodies.
+// tensor-core forward/backward kernels and Adam -- both in a fixed order,
+// so equal seeds give equal samples and equal weights -- and applies it to
+// the FP32 walk.  Inference (learned.walk):
+//   1 (default): the default group walk records the band cells and
+//     nbg_learned_tc.cu evaluates the band rows on tcgen05 tensor cores;
+//   0: the warp-coherent walk in this file, with the network fused in as
+//     mma.sync batches, per body (learned.group = 0: one MLP sample per
+//     (body, cell) pair) or per warp (learned.group = 1: one sample per
+//     (warp, cell) at the warp's centroid, shared by its 32 bodies).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
