@@ -7,7 +7,9 @@ must not pay for an allocation and its device synchronisation); its scratch
 is a fixed array inside the library.  This file is collected last so that a
 run stopping at the first failure has already run every other test.  The
 first call on a device may load the library's module (CUDA's lazy loading),
-which allocates; the last test checks that later calls allocate nothing.
+which allocates; test_noalloc_first_call_in_fresh_process makes that call
+the process's first direct-sum call and checks that later calls leave the
+free device memory unchanged.
 """
 import ctypes as C
 
@@ -142,34 +144,3 @@ def test_noalloc_first_call_in_fresh_process(gpulib):
     assert r.returncode == 0, r.stdout + r.stderr
     assert "fresh ok" in r.stdout
 
-
-def test_noalloc_calls_allocate_no_device_memory(make_engine, gpulib):
-    # After the first call on the device (which may load the library's
-    # module), further calls leave the device's free memory unchanged: any
-    # cudaMalloc takes at least one 2 MiB page, so a drop below 2 MiB means
-    # none happened.
-    torch = pytest.importorskip("torch")
-    n = 4096
-    d = NBodyData.plummer(n, seed=4)
-    e = make_engine(precision="mixed", softening=1e-3)
-    assert e.init(d)
-    y = e.create_buffer(8 * 6 * n)
-    m = e.create_buffer(8 * n)
-    f = e.create_buffer(8 * 6 * n)
-    e.write_buffer(y, d.to_state())
-    e.write_buffer(m, np.ascontiguousarray(d.mass, dtype=np.float64))
-    stream = gpulib.nbg_stream(e.handle)
-
-    def call():
-        st = gpulib.nbg_direct_mixed_noalloc(y.device_ptr(), m.device_ptr(), f.device_ptr(),
-                                             n, 1e-3, stream)
-        assert st == 0, gpulib.nbg_status_string(st)
-
-    call()
-    e.synchronize()
-    free0, _ = torch.cuda.mem_get_info()
-    for _ in range(3):
-        call()
-    e.synchronize()
-    free1, _ = torch.cuda.mem_get_info()
-    assert free0 - free1 < (2 << 20), (free0, free1)
