@@ -252,10 +252,11 @@ nbg_status nbg_learn_predict(nbg_engine* e, const float* x, size_t count, float*
  * accumulators in tensor memory.  count <= 2^30. */
 nbg_status nbg_learn_predict_tc(nbg_engine* e, const float* x, size_t count, float* out);
 /* For checks of the tcgen05 layouts: each row's tensor-memory accumulators
- * of that forward pass, acc [count][144]: the first layer's D1 = X W1
- * (0..63), the second layer's D2 = GELU(D1 + b1) W2 (64..127) and the
- * third layer's D3 = GELU(D2 + b2) W3 (128..143; 131..143 zero), biases
- * not added. */
+ * of that forward pass, acc [count][144]: the first layer's D1 = X W1 + b1
+ * (0..63), the second layer's D2 = GELU(D1) W2 + b2 (64..127) and the
+ * third layer's D3 = GELU(D2) W3 + b3 (128..143; 131..143 zero); each
+ * bias is added by the tensor core, as three BF16 terms against a block of
+ * ones. */
 nbg_status nbg_learn_tc_accumulators(nbg_engine* e, const float* x, size_t count, float* acc);
 /* The judge's figures: out[0] engine step judged last, [1] p50 and [2] p99
  * relative error of the learned forces, [3] p50 and [4] p99 of the plain

@@ -15,13 +15,17 @@ namespace nbg {
 // with more is walked body by body instead.
 constexpr int kCandCap = 2048;
 // tcgen05 operand block: W1^T (64 x 16), W2^T / 2 (64 x 64), W3^T / 2
-// (16 x 64, rows past 3 zero) as K-major BF16 core matrices, then the
-// biases b1[64], b2[64], b3[16] (FP32, past 3 zero).
+// (16 x 64, rows past 3 zero) as K-major BF16 core matrices, then the bias
+// operands B1 (64 x 16), B2 (64 x 16), B3 (16 x 16): row n holds the bias
+// of output n split into three BF16 terms (columns 0-2, the rest zero),
+// which a K = 16 MMA against a block of ones adds to the accumulator.
 constexpr int kTcwW1 = 0;                  // words
 constexpr int kTcwW2 = kTcwW1 + 64 * 16 / 2;
 constexpr int kTcwW3 = kTcwW2 + 64 * 64 / 2;
-constexpr int kTcwBias = kTcwW3 + 16 * 64 / 2;
-constexpr int kTcwWords = kTcwBias + 64 + 64 + 16;
+constexpr int kTcwB1 = kTcwW3 + 16 * 64 / 2;
+constexpr int kTcwB2 = kTcwB1 + 64 * 16 / 2;
+constexpr int kTcwB3 = kTcwB2 + 64 * 16 / 2;
+constexpr int kTcwWords = kTcwB3 + 16 * 16 / 2;
 
 struct LearnState {
     // model
@@ -55,7 +59,7 @@ struct LearnState {
     uint64_t judged = 0, fallbacks = 0;
     JudgeResult last;
     // tensor-core (tcgen05) inference on the group walk (nbg_learned_tc.cu):
-    // the weights as K-major BF16 operands and the padded biases, kTcwWords
+    // the weights and biases as K-major BF16 operands, kTcwWords
     // words; each group's band cells; the kernel's next group
     uint32_t* tcw = nullptr;
     int* cand = nullptr;         // [groups][kCandCap] band cells of each group

@@ -15,13 +15,15 @@
 //    and the band pairs are compacted into 128-row tiles in shared memory.
 //    Thread r builds row r's 16 features, and the CTA evaluates the tile
 //    with three chains of tcgen05 MMAs (M = 128; N = 64, 64, 16; K = 16, 64,
-//    64), BF16 operands in shared memory, FP32 accumulators in 64 TMEM
-//    columns (each layer's over the previous one's).  Between layers each
-//    thread loads its row's accumulators (tcgen05.ld), adds the bias,
-//    applies GELU and writes the BF16 activations as the next layer's A
-//    operand.  The group's band cells pass through shared memory 64 at a
-//    time, with 1 / s and m / s^2 formed once per cell; 6 CTAs per SM.  The output head turns the
-//    three coefficients into the correction, scaled by the cell's m / s^2.
+//    64, each followed by a K = 16 MMA that adds the layer's bias: a block
+//    of ones against the bias split into three BF16 terms), BF16 operands
+//    in shared memory, FP32 accumulators in 64 TMEM columns (each layer's
+//    over the previous one's).  Between layers each thread loads its row's
+//    accumulators (tcgen05.ld), applies GELU and writes the BF16
+//    activations as the next layer's A operand.  The group's band cells
+//    pass through shared memory 64 at a time, with 1 / s and m / s^2 formed
+//    once per cell; 5 CTAs per SM.  The output head turns the three
+//    coefficients into the correction, scaled by the cell's m / s^2.
 // 3. A body's rows are contiguous (body-major order), so a segmented scan in
 //    each warp and four warp-ordered additions sum them into the group's
 //    per-body accumulators in a fixed order: equal inputs give equal
@@ -46,7 +48,7 @@ constexpr int kTcRows = 128;         // rows per tile (the MMA's M)
 // TMEM columns: each layer's accumulator (64, 64, 16 columns) at column 0,
 // written once every thread has read the previous layer's
 constexpr int kTcCols = 64;
-constexpr int kTcBlocksPerSm = 6;    // as shared memory allows; 6 x 64 of the SM's 512 columns
+constexpr int kTcBlocksPerSm = 5;    // as shared memory allows; 5 x 64 of the SM's 512 columns
 constexpr int kGroupBodies = 64;     // bodies of a group (the default group walk)
 constexpr int kCellChunk = 64;       // band cells staged in shared memory at a time
 static_assert(kCellChunk == 64, "the full-chunk index split is a shift by 6");
@@ -56,7 +58,9 @@ constexpr size_t kTcSmemFloor = 26 * 1024;
 constexpr int kDumpCols = 144;       // accumulator dump: D1 (64), D2 (64), D3 (16)
 
 struct TcSmem {
-    uint32_t w[kTcwWords];  // operands W1^T, W2^T, W3^T; biases
+    uint32_t w[kTcwWords];  // operands W1^T, W2^T, W3^T and the bias operands B1, B2, B3
+    // A operand of the bias MMAs (128 x 16): ones in columns 0-2, zeros after
+    alignas(128) uint32_t ones[kTcRows * 16 / 2];
     // A operands: layer 1's (K = 16, 4 KB) in the first part of layers 2
     // and 3's (K = 64, 16 KB), which the layer-1 epilogue writes only after
     // the layer-1 MMA has completed
@@ -83,6 +87,11 @@ size_t tc_smem_bytes() { return std::max(sizeof(TcSmem), kTcSmemFloor); }
 // ---------------------------------------------------------------------------
 // operands from the FP32 master weights
 // ---------------------------------------------------------------------------
+// x rounded to the nearest BF16 value, as a float.
+__device__ __forceinline__ float bf16_round(float x) {
+    return __uint_as_float(pack_bf16(x, 0.f) << 16);
+}
+
 // One thread per BF16 pair (k, k + 1) of one operand row n.  W2 and W3
 // carry GELU's factor 1/2 (exact in BF16): the epilogue forms 2 GELU(z) =
 // z + z tanh(u) with one FMA, and the products are the same bit for bit.
@@ -102,26 +111,43 @@ __global__ void make_tc_weights_kernel(const float* __restrict__ w, uint32_t* __
         const float lo = n < kOut ? 0.5f * w[kOffW3 + k * kOut + n] : 0.f;
         const float hi = n < kOut ? 0.5f * w[kOffW3 + (k + 1) * kOut + n] : 0.f;
         tcw[kTcwW3 + tc::kmajor_offset(n, k, 64) / 4] = pack_bf16(lo, hi);
-    } else if (q < q3 + 144) {  // biases b1[64], b2[64], b3[16]
+    } else if (q < q3 + 144) {  // bias operands: rows of B1 (64), B2 (64), B3 (16)
         const int i = q - q3;
         float b = 0.f;
-        if (i < 64) b = w[kOffB1 + i];
-        else if (i < 128) b = w[kOffB2 + i - 64];
-        else if (i - 128 < kOut) b = w[kOffB3 + i - 128];
-        tcw[kTcwBias + i] = __float_as_uint(b);
+        int base = kTcwB1, n = i;
+        if (i < 64) {
+            b = w[kOffB1 + i];
+        } else if (i < 128) {
+            b = w[kOffB2 + i - 64];
+            base = kTcwB2;
+            n = i - 64;
+        } else {
+            b = i - 128 < kOut ? w[kOffB3 + i - 128] : 0.f;
+            base = kTcwB3;
+            n = i - 128;
+        }
+        // b = hi + mid + lo: each term the BF16 rounding of what the earlier
+        // ones leave (the residuals are exact in FP32), 24 bits in all
+        const float hi = bf16_round(b);
+        const float mid = bf16_round(b - hi);
+        const float lo = bf16_round((b - hi) - mid);
+        tcw[base + tc::kmajor_offset(n, 0, 16) / 4] = pack_bf16(hi, mid);
+        tcw[base + tc::kmajor_offset(n, 2, 16) / 4] = pack_bf16(lo, 0.f);
+#pragma unroll
+        for (int k = 4; k < 16; k += 2) tcw[base + tc::kmajor_offset(n, k, 16) / 4] = 0u;
     }
 }
 
 // ---------------------------------------------------------------------------
 // one 128-row tile through the network
 // ---------------------------------------------------------------------------
-// Twice the GELU of two pre-activations z = acc + bias, packed FP32x2, as
-// BF16x2: z (1 + tanh(z (c0 + c1 z^2))), c0 = sqrt(2/pi), c1 = 0.044715 c0
-// (the tanh form of nbg_mlp.cuh with the cubic factored), MUFU
-// tanh.approx.f32; the next layer's weights carry the factor 1/2.
-__device__ __forceinline__ uint32_t gelu2_bf16(f2_t acc, f2_t bias) {
+// Twice the GELU of two pre-activations z (the accumulators, biases
+// included), packed FP32x2, as BF16x2: z (1 + tanh(z (c0 + c1 z^2))),
+// c0 = sqrt(2/pi), c1 = 0.044715 c0 (the tanh form of nbg_mlp.cuh with the
+// cubic factored), MUFU tanh.approx.f32; the next layer's weights carry the
+// factor 1/2.
+__device__ __forceinline__ uint32_t gelu2_bf16(f2_t z) {
     constexpr float c0 = kGeluC, c1 = kGeluC * kGeluA;
-    const f2_t z = f2_add(acc, bias);
     const f2_t u = f2_mul(z, f2_fma(f2_pack(c1, c1), f2_mul(z, z), f2_pack(c0, c0)));
     float ua, ub;
     f2_unpack(u, ua, ub);
@@ -131,31 +157,21 @@ __device__ __forceinline__ uint32_t gelu2_bf16(f2_t acc, f2_t bias) {
     return pack_bf16(ga, gb);
 }
 
-// The warp's rows' 64 accumulator columns -> bias, GELU -> BF16 row `row`
-// of the K = 64 operand a2; dump (when not null) receives the raw values.
-__device__ __forceinline__ void hidden_to_operand(uint32_t taddr, const float* bias, uint32_t* a2,
-                                                  int row, float* dump) {
+// The warp's rows' 64 accumulator columns (biases included) -> GELU ->
+// BF16 row `row` of the K = 64 operand a2; dump (when not null) receives the
+// accumulators.
+__device__ __forceinline__ void hidden_to_operand(uint32_t taddr, uint32_t* a2, int row,
+                                                  float* dump) {
     unsigned char* base = reinterpret_cast<unsigned char*>(a2);
-    const float4* bias4 = reinterpret_cast<const float4*>(bias);  // 16-byte aligned
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         float v[16];
         tc::ld16(taddr + 16 * j, v);
         if (dump != nullptr)
             for (int q = 0; q < 16; ++q) dump[16 * j + q] = v[q];
-        float b[16];  // the 16 columns' biases, four 128-bit shared loads
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const float4 w = bias4[4 * j + q];
-            b[4 * q] = w.x;
-            b[4 * q + 1] = w.y;
-            b[4 * q + 2] = w.z;
-            b[4 * q + 3] = w.w;
-        }
         uint32_t p[8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
-            p[i] = gelu2_bf16(f2_pack(v[2 * i], v[2 * i + 1]), f2_pack(b[2 * i], b[2 * i + 1]));
+        for (int i = 0; i < 8; ++i) p[i] = gelu2_bf16(f2_pack(v[2 * i], v[2 * i + 1]));
         *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, 16 * j, 64)) =
             make_uint4(p[0], p[1], p[2], p[3]);
         *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, 16 * j + 8, 64)) =
@@ -187,10 +203,11 @@ __device__ __forceinline__ void tile_wait(TcSmem& S, uint32_t& phase, unsigned* 
 }
 
 // Issue (one thread) and complete the MMAs of one layer after the CTA's
-// operand writes: D (TMEM column 0) = A (K = 16 kk_count) x B^T.
+// operand writes: D (TMEM column 0) = A (K = 16 kk_count) x B^T, then
+// D += ones x bias^T (K = 16: the bias operand's three terms per column).
 __device__ __forceinline__ void tile_layer(TcSmem& S, uint32_t tmem, uint32_t& phase, int tid,
                                            unsigned* err, uint32_t a, uint32_t b, uint32_t sbo,
-                                           int kk_count, uint32_t idesc) {
+                                           int kk_count, uint32_t bias_b, uint32_t idesc) {
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
@@ -199,39 +216,41 @@ __device__ __forceinline__ void tile_layer(TcSmem& S, uint32_t tmem, uint32_t& p
         for (int kk = 0; kk < kk_count; ++kk)
             tc::mma_bf16(tmem, tc::smem_desc(a + 256 * kk, 128, sbo),
                          tc::smem_desc(b + 256 * kk, 128, sbo), idesc, kk > 0 ? 1u : 0u);
+        tc::mma_bf16(tmem, tc::smem_desc(smem_addr(S.ones), 128, 256),
+                     tc::smem_desc(bias_b, 128, 256), idesc, 1u);
         tc::commit(&S.mbar);
     }
     tile_wait(S, phase, err);
 }
 
 // The tile whose features every thread has written (features_to_operand):
-// three layers; returns row `tid`'s three outputs (b3 added).  Every thread
-// of the CTA calls it (it synchronises the CTA three times).  dump (when
-// not null): the row's D1, D2 and D3 accumulators, kDumpCols floats.
+// three layers; returns row `tid`'s three outputs.  Every thread of the CTA
+// calls it (it synchronises the CTA three times).  dump (when not null): the
+// row's D1, D2 and D3 accumulators (biases included), kDumpCols floats.
 __device__ __forceinline__ void tile_forward(TcSmem& S, uint32_t tmem, uint32_t& phase, int tid,
                                              unsigned* err, float out[3], float* dump) {
     const uint32_t lane_base = (uint32_t)((tid >> 5) * 32) << 16;
-    const float* b1 = reinterpret_cast<const float*>(S.w + kTcwBias);
-    const float* b2 = b1 + 64;
-    const float* b3 = b2 + 64;
     constexpr uint32_t id64 = tc::idesc_bf16_f32(kTcRows, 64);
     constexpr uint32_t id16 = tc::idesc_bf16_f32(kTcRows, 16);
     const uint32_t a = smem_addr(S.a2);
-    // layer 1: D1 = X W1 (K = 16)
-    tile_layer(S, tmem, phase, tid, err, a, smem_addr(S.w + kTcwW1), 256, 1, id64);
-    hidden_to_operand(tmem + lane_base, b1, S.a2, tid, dump);
-    // layer 2: D2 = GELU(D1 + b1) W2 (K = 64), over D1's columns
-    tile_layer(S, tmem, phase, tid, err, a, smem_addr(S.w + kTcwW2), 1024, 4, id64);
-    hidden_to_operand(tmem + lane_base, b2, S.a2, tid, dump != nullptr ? dump + 64 : nullptr);
-    // layer 3: D3 = GELU(D2 + b2) W3 (N = 16, rows past 3 zero)
-    tile_layer(S, tmem, phase, tid, err, a, smem_addr(S.w + kTcwW3), 1024, 4, id16);
+    // layer 1: D1 = X W1 + b1 (K = 16)
+    tile_layer(S, tmem, phase, tid, err, a, smem_addr(S.w + kTcwW1), 256, 1,
+               smem_addr(S.w + kTcwB1), id64);
+    hidden_to_operand(tmem + lane_base, S.a2, tid, dump);
+    // layer 2: D2 = GELU(D1) W2 + b2 (K = 64), over D1's columns
+    tile_layer(S, tmem, phase, tid, err, a, smem_addr(S.w + kTcwW2), 1024, 4,
+               smem_addr(S.w + kTcwB2), id64);
+    hidden_to_operand(tmem + lane_base, S.a2, tid, dump != nullptr ? dump + 64 : nullptr);
+    // layer 3: D3 = GELU(D2) W3 + b3 (N = 16, rows past 3 zero)
+    tile_layer(S, tmem, phase, tid, err, a, smem_addr(S.w + kTcwW3), 1024, 4,
+               smem_addr(S.w + kTcwB3), id16);
     float v[16];
     tc::ld16(tmem + lane_base, v);
     if (dump != nullptr)
         for (int q = 0; q < 16; ++q) dump[128 + q] = v[q];
-    out[0] = v[0] + b3[0];
-    out[1] = v[1] + b3[1];
-    out[2] = v[2] + b3[2];
+    out[0] = v[0];
+    out[1] = v[1];
+    out[2] = v[2];
 }
 
 // CTA setup shared by the tensor-core kernels: TMEM, operands, mbarrier.
@@ -242,6 +261,12 @@ __device__ __forceinline__ uint32_t tc_setup(TcSmem& S, const uint32_t* __restri
         tc::tmem_relinquish();
     }
     for (int i = tid; i < kTcwWords; i += kTcThreads) S.w[i] = __ldg(&tcw[i]);
+    // the ones block: row r, columns (2 p, 2 p + 1) -> word p of the row
+    for (int i = tid; i < kTcRows * 8; i += kTcThreads) {
+        const int r = i >> 3, k = 2 * (i & 7);
+        S.ones[tc::kmajor_offset(r, k, 16) / 4] =
+            pack_bf16(k < 3 ? 1.f : 0.f, k + 1 < 3 ? 1.f : 0.f);
+    }
     if (tid == 0) {
         mbar_init(&S.mbar, 1);
         S.abort = 0;
@@ -431,7 +456,7 @@ learned_tc_kernel(double* __restrict__ f, int n, int groups, TreeState t,
 
 // Network outputs of given feature rows on the tensor cores (128 rows per
 // unit), for the check against the mma.sync path.  With acc_out, each row's
-// accumulators as well (kDumpCols floats: D1, D2, D3 before their biases),
+// accumulators as well (kDumpCols floats: D1, D2, D3, biases included),
 // which check the operand, descriptor and tensor-memory layouts layer by
 // layer.
 __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm)

@@ -548,7 +548,7 @@ class NbodyEngineGB300:
 
     def learn_tc_accumulators(self, x) -> np.ndarray:
         """[count, 144]: the tcgen05 forward pass's accumulators, D1 (columns
-        0..63), D2 (64..127) and D3 (128..143), biases not added."""
+        0..63), D2 (64..127) and D3 (128..143), biases included."""
         x = np.ascontiguousarray(x, dtype=np.float32)
         out = np.zeros((x.shape[0], 144), dtype=np.float32)
         fp = C.POINTER(C.c_float)

@@ -201,25 +201,27 @@ def _features(count, seed):
 def test_tensor_core_layouts(make_engine):
     """The tcgen05 operand, instruction-descriptor and tensor-memory layouts,
     layer by layer, on random weights with nonzero biases: the accumulators
-    D1 = X W1, D2 = GELU(D1 + b1) W2 and D3 = GELU(D2 + b2) W3 (columns
-    past 3 zero).  D1 is a sum of 16 exact BF16 products in FP32; the next
-    layers are checked from the GPU's own previous accumulators (whose GELU
-    rounds to BF16 the same way)."""
+    D1 = X W1 + b1, D2 = GELU(D1) W2 + b2 and D3 = GELU(D2) W3 + b3
+    (columns past 3 zero; each bias enters as three BF16 terms through a
+    K = 16 MMA against a block of ones, exact to FP32).  D1 is a sum of 16
+    exact BF16 products and the bias in FP32; the next layers are checked
+    from the GPU's own previous accumulators (whose GELU rounds to BF16 the
+    same way)."""
     e = _bh_engine(make_engine, 1.0 / 0.9, learned=True)
     assert e.init(NBodyData.plummer(1024, seed=1))
     w = _random_weights(3)
     e.learn_set_weights(w)
     W1, _, W2, _, W3, _ = M.unpack(M.bf16(w))
-    b1, b2 = M.unpack(w)[1], M.unpack(w)[3]  # biases stay FP32
+    b1, b2, b3 = M.unpack(w)[1], M.unpack(w)[3], M.unpack(w)[5]  # biases stay FP32
     for count in (1, 200, 4096):
         x = _features(count, 11 + count)
         acc = e.learn_tc_accumulators(x).astype(np.float64)
         d1, d2, d3 = acc[:, 0:64], acc[:, 64:128], acc[:, 128:144]
         xb = M.bf16(x)
-        err1 = np.abs(d1 - xb @ W1) / (np.abs(xb) @ np.abs(W1) + 1e-30)
-        z2 = M.bf16(M.gelu(d1 + b1)) @ W2
+        err1 = np.abs(d1 - (xb @ W1 + b1)) / (np.abs(xb) @ np.abs(W1) + np.abs(b1) + 1e-30)
+        z2 = M.bf16(M.gelu(d1)) @ W2 + b2
         err2 = np.linalg.norm(d2 - z2) / np.linalg.norm(z2)
-        z3 = M.bf16(M.gelu(d2 + b2)) @ W3
+        z3 = M.bf16(M.gelu(d2)) @ W3 + b3
         err3 = np.linalg.norm(d3[:, :3] - z3) / np.linalg.norm(z3)
         print(f"\ncount {count}: D1 max err / bound {err1.max():.2e}, D2 rel err {err2:.2e}, "
               f"D3 rel err {err3:.2e}")
